@@ -1,0 +1,258 @@
+"""Benchmark: DoF/s of the SIPG Laplace operator apply (FP64, k = 4, 64^3 Cartesian cells of
+[0,1]^3, all-Dirichlet, 32.8M DoF) -- the reference's operator-throughput measurement
+(poisson/driver.cpp:182-232, operators/throughput_parameters.h:40-87) on one GB300.
+
+Prints ONE JSON line.  `value` is the device-resident throughput (CUDA events on the launch
+stream), `e2e` the same metric through the public API with the input copied from pinned host
+memory and the result copied back inside the timed region.  `--impl reference` times the CPU
+oracle restatement of the same operator on the host cores (the reference itself needs deal.II,
+which is not installed).
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_CELLS = 64
+DEGREE = 4
+METRIC = "DoF/s of op apply (FP64 SIPG Laplace, k=4, 64^3 cells)"
+UNIT = "DoF/s"
+
+
+def splitmix_uniform(n, seed):
+    import numpy as np
+
+    idx = np.arange(n, dtype=np.uint64)
+    with np.errstate(over="ignore"):
+        z = (np.uint64(seed) ^ idx) + np.uint64(0x9E3779B97F4A7C15)
+        z = (z ^ (z >> np.uint64(30))) * np.uint64(0xBF58476D1CE4E5B9)
+        z = (z ^ (z >> np.uint64(27))) * np.uint64(0x94D049BB133111EB)
+        z = z ^ (z >> np.uint64(31))
+    return 2.0 * ((z >> np.uint64(11)).astype(np.float64) * (1.0 / 9007199254740992.0)) - 1.0
+
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = "clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown," \
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown," \
+             "clocks_event_reasons.sw_power_cap"
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.stop = threading.Event()
+        self.t = threading.Thread(target=self.run, daemon=True)
+
+    def run(self):
+        while not self.stop.is_set():
+            try:
+                out = subprocess.run(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                      "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                vals = [v.strip() for v in out.stdout.strip().split(",")]
+                if len(vals) >= 7:
+                    self.samples.append(vals)
+            except Exception:
+                pass
+            self.stop.wait(0.2)
+
+    def __enter__(self):
+        self.t.start()
+        return self
+
+    def __exit__(self, *a):
+        self.stop.set()
+        self.t.join(timeout=10)
+
+    def summary(self):
+        import statistics
+
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        smax = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower().startswith("active")})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {"hbm_gbs": 6800.0, "fallback": True}
+
+
+def cpu_apply_sample(threads=None, seconds=10.0):
+    """Oracle apply on a bounded sample (k = 4, 24^3 cells) on the host cores."""
+    import numpy as np
+
+    import oracle as O
+
+    if threads:
+        O.set_threads(threads)
+    n = 24
+    p = O.Problem(O.mesh_desc(n), DEGREE)
+    x = splitmix_uniform(p.n_dofs, 1)
+    p.apply(x)
+    t0 = time.perf_counter()
+    reps = 0
+    while True:
+        p.apply(x)
+        reps += 1
+        if time.perf_counter() - t0 >= seconds:
+            break
+    dt = (time.perf_counter() - t0) / reps
+    return {"value": p.n_dofs / dt, "unit": UNIT, "cores": O.max_threads(), "kind": "port",
+            "sample": "oracle FP64 apply, k=4, %d^3 cells (%d DoF), %d applies, %.1f s" % (n, p.n_dofs, reps,
+                                                                                          dt * reps)}
+
+
+def run_reference(args):
+    rank, world, local = dist_info()
+    if rank != 0:
+        return 0
+    cb = cpu_apply_sample(seconds=max(2.0, 1.0 * args.steps / 10))
+    line = {"impl": "reference", "metric": METRIC, "value": cb["value"], "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": "SIPG apply k=4 (oracle restatement sample on host cores)", "degree": DEGREE},
+            "cpu_baseline": cb,
+            "e2e": {"value": cb["value"], "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference (deal.II) not installable here; the oracle restatement is the reference arm"}
+    print(json.dumps(line))
+    return 0
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    import exadg_gb300 as E
+    from exadg_gb300 import build as B
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    B.build()
+    E.load_library()
+    prec = {"f64": E.PREC_F64, "f32": E.PREC_F32, "f64e": E.PREC_F64E}[args.precision]
+    mesh = E.Mesh(N_CELLS)
+    op = E.LaplaceOperator(mesh, DEGREE, 1.0, prec)
+    n = op.n_dofs
+    dt = op.dtype
+    esize = 4 if prec == E.PREC_F32 else 8
+    x_host = torch.tensor(splitmix_uniform(n, 1 + rank), dtype=dt).pin_memory()
+    y_host = torch.empty(n, dtype=dt).pin_memory()
+    x = x_host.to("cuda")
+    y = torch.empty_like(x)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        op.vmult(y, x)
+    barrier()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            op.vmult(y, x)
+        ev1.record(stream)
+        barrier()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([ms], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * n / (ms * 1e-3)
+
+    # e2e: host input -> device -> apply -> host output, every step
+    for _ in range(2):
+        x.copy_(x_host, non_blocking=True)
+        op.vmult(y, x)
+        y_host.copy_(y, non_blocking=True)
+    barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e2e_steps = max(3, args.steps // 10)
+    e0.record(stream)
+    for _ in range(e2e_steps):
+        x.copy_(x_host, non_blocking=True)
+        op.vmult(y, x)
+        y_host.copy_(y, non_blocking=True)
+    e1.record(stream)
+    barrier()
+    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+
+    pk = peaks()
+    bytes_per_apply = 2.0 * esize * n
+    achieved = bytes_per_apply / (ms * 1e-3) / 1e9
+    out = None
+    if rank == 0:
+        cb = cpu_apply_sample(seconds=10.0) if not args.no_cpu_baseline else None
+        out = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": {"f64": "f64", "f32": "f32", "f64e": "f64 (FP32-pair arithmetic)"}[args.precision],
+            "data": "synthetic",
+            "config": {"workload": "SIPG Laplace apply, Cartesian 64^3 cells of [0,1]^3, all Dirichlet, k=%d" % DEGREE,
+                       "degree": DEGREE, "n_cells": N_CELLS ** 3, "n_dofs": n, "precision": args.precision,
+                       "parallelism": "replicas" if world > 1 else "single GPU",
+                       "l2": "inputs larger than L2 (src+dst %.0f MB > 129 MB)" % (bytes_per_apply / 1e6)},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
+                         "frac": achieved / pk.get("hbm_gbs", 6800.0), "traffic": None,
+                         "note": "algorithmic bytes = 2 x %d B x n_dofs per apply (src read + dst write)" % esize},
+            "cpu_baseline": cb,
+            "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": esize * n,
+                    "d2h_bytes_per_step": esize * n},
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(out))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--precision", default="f64", choices=["f64", "f32", "f64e"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,365 @@
+"""exadg_gb300 -- GB300-native matrix-free SIPG Laplace operator, multigrid and CG.
+
+Python mirror of ExaDG's Poisson interfaces on top of the C ABI in ``include/exadg_gb300.h``
+(``exadg_gb300/_lib/libexadg_gb300.so``).  Device vectors are torch CUDA tensors; torch is used
+only for device memory and streams.  There is no CPU fallback: without the compiled library or a
+GPU the classes raise.
+
+Reference interfaces mirrored (paths relative to the ExaDG tree):
+  LaplaceOperator.vmult / calculate_inverse_diagonal / rhs
+      poisson/spatial_discretization/laplace_operator.h:228-350, operators/operator_base.h:175-213
+  MultigridPreconditioner.vmult / update
+      poisson/preconditioners/multigrid_preconditioner.cpp:37-149,
+      solvers_and_preconditioners/preconditioners/preconditioner_base.h:33-67
+  KrylovSolver.solve
+      solvers_and_preconditioners/solvers/iterative_solvers_dealii_wrapper.h:136-221
+"""
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_lib", "libexadg_gb300.so")
+
+EXG_OK = 0
+EXG_ERR_INVALID = 1
+EXG_ERR_CUDA = 2
+EXG_ERR_NOT_CONVERGED = 3
+EXG_ERR_NONFINITE = 4
+EXG_ERR_UNSUPPORTED = 5
+EXG_ERR_NEEDS_UPDATE = 6
+
+PREC_F64 = 0
+PREC_F32 = 1
+PREC_F64E = 2
+
+BC_DIRICHLET = 0
+BC_NEUMANN = 1
+
+
+class ExgError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__("exadg_gb300 status %d: %s" % (status, msg))
+        self.status = status
+
+
+class MeshDesc(ctypes.Structure):
+    _fields_ = [
+        ("n_cells", ctypes.c_int * 3),
+        ("lo", ctypes.c_double * 3),
+        ("hi", ctypes.c_double * 3),
+        ("periodic", ctypes.c_int * 3),
+        ("bc", ctypes.c_int * 6),
+        ("deform_amp", ctypes.c_double),
+        ("deform_freq", ctypes.c_int),
+        ("deform_left", ctypes.c_double),
+        ("deform_right", ctypes.c_double),
+        ("mapping_degree", ctypes.c_int),
+    ]
+
+
+class MGDesc(ctypes.Structure):
+    _fields_ = [
+        ("mg_precision", ctypes.c_int),
+        ("cheb_degree", ctypes.c_int),
+        ("smoothing_range", ctypes.c_double),
+        ("eig_iters", ctypes.c_int),
+        ("coarse_rel_tol", ctypes.c_double),
+        ("coarse_abs_tol", ctypes.c_double),
+        ("coarse_max_iter", ctypes.c_int),
+        ("coarse_double", ctypes.c_int),
+        ("min_coarse_cells", ctypes.c_int),
+        ("singular", ctypes.c_int),
+        ("use_graph", ctypes.c_int),
+    ]
+
+
+class MGInfo(ctypes.Structure):
+    _fields_ = [
+        ("n_levels", ctypes.c_int),
+        ("degree", ctypes.c_int * 32),
+        ("n_cells", (ctypes.c_int * 3) * 32),
+        ("lambda_max", ctypes.c_double * 32),
+        ("eig_iters", ctypes.c_int * 32),
+        ("coarse_iterations", ctypes.c_longlong),
+        ("vcycles", ctypes.c_longlong),
+    ]
+
+
+class CGDesc(ctypes.Structure):
+    _fields_ = [
+        ("max_iter", ctypes.c_int),
+        ("abs_tol", ctypes.c_double),
+        ("rel_tol", ctypes.c_double),
+        ("precond", ctypes.c_int),
+    ]
+
+
+class CGResult(ctypes.Structure):
+    _fields_ = [
+        ("iterations", ctypes.c_int),
+        ("converged", ctypes.c_int),
+        ("r0", ctypes.c_double),
+        ("rn", ctypes.c_double),
+        ("rho", ctypes.c_double),
+        ("n10", ctypes.c_double),
+        ("seconds", ctypes.c_double),
+    ]
+
+
+# every symbol declared in include/exadg_gb300.h
+EXPORTED_SYMBOLS = [
+    "exg_mesh_create", "exg_mesh_destroy", "exg_sipg_create", "exg_sipg_destroy", "exg_sipg_n_dofs",
+    "exg_sipg_info", "exg_sipg_apply_f64", "exg_sipg_apply_f32", "exg_sipg_inverse_diagonal_f64",
+    "exg_sipg_inverse_diagonal_f32", "exg_sipg_quadrature_points", "exg_sipg_rhs", "exg_mg_default_desc",
+    "exg_mg_create", "exg_mg_destroy", "exg_mg_vmult", "exg_mg_info_get", "exg_cg_default_desc", "exg_cg_solve",
+    "exg_status_string", "exg_last_error",
+]
+
+_lib = None
+
+
+def load_library(path=LIB_PATH):
+    """Load the compiled library (raises if it is missing: there is no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ExgError(EXG_ERR_INVALID, "compiled library %s not found; run exadg_gb300.build.build()" % path)
+    L = ctypes.CDLL(path)
+    P = ctypes.c_void_p
+    I = ctypes.c_int
+    D = ctypes.c_double
+    LL = ctypes.c_longlong
+    PP = ctypes.POINTER(ctypes.c_void_p)
+    sig = {
+        "exg_mesh_create": [ctypes.POINTER(MeshDesc), PP],
+        "exg_mesh_destroy": [P],
+        "exg_sipg_create": [P, I, D, I, PP],
+        "exg_sipg_destroy": [P],
+        "exg_sipg_n_dofs": [P, ctypes.POINTER(LL)],
+        "exg_sipg_info": [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)],
+        "exg_sipg_apply_f64": [P, P, P, I, P],
+        "exg_sipg_apply_f32": [P, P, P, I, P],
+        "exg_sipg_inverse_diagonal_f64": [P, P, P],
+        "exg_sipg_inverse_diagonal_f32": [P, P, P],
+        "exg_sipg_quadrature_points": [P, P, P, ctypes.POINTER(LL), ctypes.POINTER(LL), P],
+        "exg_sipg_rhs": [P, P, P, P, P, P],
+        "exg_mg_default_desc": [ctypes.POINTER(MGDesc)],
+        "exg_mg_create": [P, ctypes.POINTER(MGDesc), PP],
+        "exg_mg_destroy": [P],
+        "exg_mg_vmult": [P, P, P, P],
+        "exg_mg_info_get": [P, ctypes.POINTER(MGInfo)],
+        "exg_cg_default_desc": [ctypes.POINTER(CGDesc)],
+        "exg_cg_solve": [P, P, ctypes.POINTER(CGDesc), P, P, ctypes.POINTER(CGResult), P],
+    }
+    for name, args in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = ctypes.c_int
+    L.exg_status_string.argtypes = [ctypes.c_int]
+    L.exg_status_string.restype = ctypes.c_char_p
+    L.exg_last_error.argtypes = []
+    L.exg_last_error.restype = ctypes.c_char_p
+    _lib = L
+    return L
+
+
+def _check(status):
+    if status != EXG_OK:
+        L = load_library()
+        raise ExgError(status, L.exg_last_error().decode())
+
+
+def _ptr(t):
+    if t is None:
+        return None
+    import torch
+
+    if not isinstance(t, torch.Tensor) or not t.is_cuda:
+        raise ExgError(EXG_ERR_INVALID, "expected a CUDA tensor")
+    if not t.is_contiguous():
+        raise ExgError(EXG_ERR_INVALID, "expected a contiguous tensor")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _stream(stream=None):
+    import torch
+
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return ctypes.c_void_p(s.cuda_stream)
+
+
+class Mesh:
+    """Structured hex mesh of a box (subdivided_hyper_rectangle), optional DeformedCubeManifold."""
+
+    def __init__(self, n_cells, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0), periodic=(0, 0, 0), bc=(0,) * 6,
+                 deform_amp=0.0, deform_freq=1, deform_left=0.0, deform_right=1.0, mapping_degree=1):
+        if isinstance(n_cells, int):
+            n_cells = (n_cells,) * 3
+        d = MeshDesc()
+        d.n_cells[:] = list(n_cells)
+        d.lo[:] = list(lo)
+        d.hi[:] = list(hi)
+        d.periodic[:] = list(periodic)
+        d.bc[:] = list(bc)
+        d.deform_amp = deform_amp
+        d.deform_freq = deform_freq
+        d.deform_left = deform_left
+        d.deform_right = deform_right
+        d.mapping_degree = mapping_degree
+        self.desc = d
+        self.n_cells = tuple(n_cells)
+        h = ctypes.c_void_p()
+        _check(load_library().exg_mesh_create(ctypes.byref(d), ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.exg_mesh_destroy(self.h)
+            self.h = None
+
+
+class LaplaceOperator:
+    """SIPG Laplace operator (Poisson::LaplaceOperator) on FE_DGQ(degree), QGauss(degree+1)."""
+
+    def __init__(self, mesh, degree, ip_factor=1.0, precision=PREC_F64):
+        self.mesh = mesh
+        self.degree = degree
+        self.precision = precision
+        h = ctypes.c_void_p()
+        _check(load_library().exg_sipg_create(mesh.h, degree, ip_factor, precision, ctypes.byref(h)))
+        self.h = h
+        n = ctypes.c_longlong()
+        _check(_lib.exg_sipg_n_dofs(h, ctypes.byref(n)))
+        self.n_dofs = n.value
+        c = ctypes.c_int()
+        _check(_lib.exg_sipg_info(h, None, None, ctypes.byref(c)))
+        self.cartesian = bool(c.value)
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.exg_sipg_destroy(self.h)
+            self.h = None
+
+    @property
+    def dtype(self):
+        import torch
+
+        return torch.float32 if self.precision == PREC_F32 else torch.float64
+
+    def initialize_dof_vector(self, n_rhs=1):
+        import torch
+
+        shape = (self.n_dofs,) if n_rhs == 1 else (n_rhs, self.n_dofs)
+        return torch.zeros(shape, dtype=self.dtype, device="cuda")
+
+    def vmult(self, dst, src, n_rhs=1, stream=None):
+        """dst = A src (dst overwritten), operator_base.cpp:156-168."""
+        f = _lib.exg_sipg_apply_f32 if self.precision == PREC_F32 else _lib.exg_sipg_apply_f64
+        _check(f(self.h, _ptr(src), _ptr(dst), n_rhs, _stream(stream)))
+        return dst
+
+    apply = vmult
+
+    def calculate_inverse_diagonal(self, diag, stream=None):
+        f = _lib.exg_sipg_inverse_diagonal_f32 if self.precision == PREC_F32 else _lib.exg_sipg_inverse_diagonal_f64
+        _check(f(self.h, _ptr(diag), _stream(stream)))
+        return diag
+
+    def quadrature_points(self, stream=None):
+        """Cell points [n_cells, (k+1)^3, 3] and face points [n_cells, 6, (k+1)^2, 3] (FP64)."""
+        import torch
+
+        ncp = ctypes.c_longlong()
+        nfp = ctypes.c_longlong()
+        _check(_lib.exg_sipg_quadrature_points(self.h, None, None, ctypes.byref(ncp), ctypes.byref(nfp),
+                                               _stream(stream)))
+        cx = torch.empty((ncp.value, 3), dtype=torch.float64, device="cuda")
+        fx = torch.empty((nfp.value, 3), dtype=torch.float64, device="cuda")
+        _check(_lib.exg_sipg_quadrature_points(self.h, _ptr(cx), _ptr(fx), ctypes.byref(ncp), ctypes.byref(nfp),
+                                               _stream(stream)))
+        return cx, fx
+
+    def rhs(self, f_cell=None, g_face=None, h_face=None, stream=None):
+        """b = (f, v) - inhomogeneous boundary part, from function values at the quadrature points."""
+        b = self.initialize_dof_vector()
+        _check(_lib.exg_sipg_rhs(self.h, _ptr(f_cell), _ptr(g_face), _ptr(h_face), _ptr(b), _stream(stream)))
+        return b
+
+
+class MultigridPreconditioner:
+    """phMG V-cycle preconditioner (MultigridPreconditionerBase::vmult)."""
+
+    def __init__(self, operator, mg_precision=PREC_F32, cheb_degree=5, smoothing_range=20.0, eig_iters=20,
+                 coarse_rel_tol=1e-3, coarse_abs_tol=1e-12, coarse_max_iter=10000, coarse_double=False,
+                 min_coarse_cells=2, singular=False, use_graph=True):
+        d = MGDesc()
+        _check(load_library().exg_mg_default_desc(ctypes.byref(d)))
+        d.mg_precision = mg_precision
+        d.cheb_degree = cheb_degree
+        d.smoothing_range = smoothing_range
+        d.eig_iters = eig_iters
+        d.coarse_rel_tol = coarse_rel_tol
+        d.coarse_abs_tol = coarse_abs_tol
+        d.coarse_max_iter = coarse_max_iter
+        d.coarse_double = int(coarse_double)
+        d.min_coarse_cells = min_coarse_cells
+        d.singular = int(singular)
+        d.use_graph = int(use_graph)
+        self.desc = d
+        self.operator = operator
+        h = ctypes.c_void_p()
+        _check(_lib.exg_mg_create(operator.h, ctypes.byref(d), ctypes.byref(h)))
+        self.h = h
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.exg_mg_destroy(self.h)
+            self.h = None
+
+    def vmult(self, dst, src, stream=None):
+        _check(_lib.exg_mg_vmult(self.h, _ptr(src), _ptr(dst), _stream(stream)))
+        return dst
+
+    def info(self):
+        i = MGInfo()
+        _check(_lib.exg_mg_info_get(self.h, ctypes.byref(i)))
+        return dict(
+            n_levels=i.n_levels,
+            levels=[dict(degree=i.degree[l], n_cells=tuple(i.n_cells[l]), lambda_max=i.lambda_max[l],
+                         eig_iters=i.eig_iters[l]) for l in range(i.n_levels)],
+            coarse_iterations=i.coarse_iterations,
+            vcycles=i.vcycles,
+        )
+
+
+class KrylovSolver:
+    """PCG (Krylov::KrylovSolver with SolverCG and ReductionControl)."""
+
+    NONE, JACOBI, MULTIGRID = 0, 1, 2
+
+    def __init__(self, operator, preconditioner=None, max_iter=10000, abs_tol=1e-20, rel_tol=1e-10, precond=None):
+        self.operator = operator
+        self.preconditioner = preconditioner
+        d = CGDesc()
+        _check(load_library().exg_cg_default_desc(ctypes.byref(d)))
+        d.max_iter = max_iter
+        d.abs_tol = abs_tol
+        d.rel_tol = rel_tol
+        if precond is None:
+            precond = self.MULTIGRID if preconditioner is not None else self.NONE
+        d.precond = precond
+        self.desc = d
+        self.result = None
+
+    def solve(self, dst, rhs, stream=None, raise_on_failure=True):
+        """Solve A dst = rhs with dst as the initial guess; returns the iteration count."""
+        r = CGResult()
+        mg = self.preconditioner.h if self.preconditioner is not None else None
+        st = _lib.exg_cg_solve(self.operator.h, mg, ctypes.byref(self.desc), _ptr(rhs), _ptr(dst), ctypes.byref(r),
+                               _stream(stream))
+        self.result = dict(iterations=r.iterations, converged=bool(r.converged), r0=r.r0, rn=r.rn, rho=r.rho,
+                           n10=r.n10, seconds=r.seconds, status=st)
+        if st != EXG_OK and raise_on_failure:
+            _check(st)
+        return r.iterations

@@ -1,0 +1,534 @@
+// Host orchestration: operator set-up and dispatch, the multigrid hierarchy (phMG, Bisect,
+// Chebyshev-Jacobi, coarse CG, V-cycle as a CUDA graph) and the outer PCG.
+#include "host.h"
+
+#include <algorithm>
+#include <array>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+namespace exg {
+
+MeshInfo make_mesh_info(const exg_mesh_desc& d) {
+  MeshInfo m;
+  m.d = d;
+  for (int e = 0; e < 3; ++e) {
+    EXG_CHECK(d.n_cells[e] >= 1, EXG_ERR_INVALID, "n_cells must be >= 1");
+    EXG_CHECK(d.hi[e] > d.lo[e], EXG_ERR_INVALID, "box must have positive extent");
+    m.N[e] = d.n_cells[e];
+    m.h[e] = (d.hi[e] - d.lo[e]) / d.n_cells[e];
+    if (d.deform_amp != 0.0)
+      EXG_CHECK(!d.periodic[e], EXG_ERR_UNSUPPORTED, "periodic directions need an affine mesh");
+  }
+  for (int f = 0; f < 6; ++f)
+    EXG_CHECK(d.bc[f] == EXG_BC_DIRICHLET || d.bc[f] == EXG_BC_NEUMANN, EXG_ERR_INVALID, "bad boundary type");
+  return m;
+}
+
+// --------------------------------------------------------------------------------------------
+// deterministic scalar readback
+// --------------------------------------------------------------------------------------------
+static double read_slot(Reduction& red, int slot, cudaStream_t s) {
+  double v;
+  EXG_CUDA(cudaMemcpyAsync(&v, red.out + slot, sizeof(double), cudaMemcpyDeviceToHost, s));
+  EXG_CUDA(cudaStreamSynchronize(s));
+  return v;
+}
+
+static size_t psize(int prec) { return prec == EXG_PREC_F32 ? sizeof(float) : sizeof(double); }
+
+static void* dalloc(size_t bytes) {
+  void* p = nullptr;
+  EXG_CUDA(cudaMalloc(&p, bytes));
+  return p;
+}
+
+}  // namespace exg
+
+using namespace exg;
+
+// ============================================================================================
+// operator
+// ============================================================================================
+exg_op::exg_op(const MeshInfo& m, int deg, double ip_factor, int prec)
+    : mesh(m), degree(deg), n(deg + 1), ip(ip_factor), precision(prec) {
+  EXG_CHECK(deg >= 1 && deg <= 8, EXG_ERR_UNSUPPORTED, "degree must be 1..8");
+  EXG_CHECK(prec == EXG_PREC_F64 || prec == EXG_PREC_F32 || prec == EXG_PREC_F64E, EXG_ERR_INVALID,
+            "unknown precision");
+  EXG_CHECK(m.n_cells() * n * n * n < (1LL << 40), EXG_ERR_INVALID, "mesh too large");
+  fe.init(deg, deg + 1);
+  cartesian = m.affine();
+  build_cart_host(m, fe, ip, cart);
+  if (!cartesian) {
+    EXG_CHECK(prec != EXG_PREC_F64E, EXG_ERR_UNSUPPORTED, "FP64-emulated arithmetic is implemented for affine meshes");
+    geo.reset(new GeneralGeom());
+    geo->build(m, fe, ip, prec, false, nullptr);
+    EXG_CUDA(cudaDeviceSynchronize());
+  }
+}
+
+void exg_op::apply(const void* src, void* dst, int n_rhs, cudaStream_t s) const {
+  if (cartesian)
+    cart_apply(cart, precision, src, dst, n_rhs, cpb, s);
+  else
+    general_apply(*geo, fe, src, dst, n_rhs, s);
+}
+
+void exg_op::diagonal(void* d, bool invert, cudaStream_t s) const {
+  if (cartesian)
+    cart_diagonal(cart, precision, d, invert, s);
+  else
+    general_diagonal(*geo, fe, d, invert, s);
+}
+
+void exg_op::ensure_rhs_geometry(cudaStream_t s) {
+  if (rhs_geo) return;
+  rhs_geo.reset(new GeneralGeom());
+  rhs_geo->build(mesh, fe, ip, EXG_PREC_F64, true, s);
+  EXG_CUDA(cudaStreamSynchronize(s));
+}
+
+void exg_op::quadrature_points(double* cx, double* fx, long long* ncp, long long* nfp, cudaStream_t s) {
+  ensure_rhs_geometry(s);
+  const GeneralGeom& g = (rhs_geo ? *rhs_geo : *geo);
+  general_points(g, cx, fx, ncp, nfp, s);
+}
+
+void exg_op::rhs(const double* f, const double* g, const double* h, double* b, cudaStream_t s) {
+  ensure_rhs_geometry(s);
+  const GeneralGeom& gg = (rhs_geo ? *rhs_geo : *geo);
+  general_rhs(gg, fe, f, g, h, b, s);
+}
+
+// ============================================================================================
+// PCG driver (deal.II SolverCG + ReductionControl / IterationNumberControl semantics,
+// solvers/iterative_solvers_dealii_wrapper.h:136-221)
+// ============================================================================================
+namespace exg {
+struct CGStats {
+  int its = 0;
+  int status = 0;  // 0 converged, 1 max_iter, 2 non-finite
+  double r0 = 0, rn = 0;
+  std::vector<double> diag, offdiag;
+};
+
+template <class T, class AOp, class POp>
+static CGStats pcg_run(AOp&& A, POp&& P, const T* b, T* x, long long n, double rel, double abs, int max_iter,
+                       bool fixed, bool track, T* r, T* z, T* p, T* v, Reduction& red, cudaStream_t s) {
+  CGStats st;
+  dot<T>(x, x, n, red, 0, s);
+  bool xzero = read_slot(red, 0, s) == 0.0;
+  if (xzero)
+    residual<T>(b, nullptr, r, n, red, 1, s);
+  else {
+    A(x, v);
+    residual<T>(b, v, r, n, red, 1, s);
+  }
+  double rn = std::sqrt(read_slot(red, 1, s));
+  st.r0 = rn;
+  double tol = fixed ? abs : std::max(abs, rel * rn);
+  auto check = [&](int it, double val) -> int {
+    if (!std::isfinite(val)) return 2;
+    if (fixed) return (it >= max_iter || val <= tol) ? 0 : -1;
+    if (val <= tol) return 0;
+    if (it >= max_iter) return 1;
+    return -1;
+  };
+  int c = check(0, rn);
+  int it = 0;
+  double rho_old = 0, alpha_old = 0;
+  while (c < 0) {
+    ++it;
+    double rho = P(r, z);
+    double beta = it == 1 ? 0.0 : rho / rho_old;
+    p_update<T>(z, p, beta, it == 1, n, s);
+    A(p, v);
+    dot<T>(p, v, n, red, 2, s);
+    double pv = read_slot(red, 2, s);
+    double alpha = rho / pv;
+    xr_update<T>(x, r, p, v, alpha, n, red, 3, s);
+    rn = std::sqrt(read_slot(red, 3, s));
+    if (track) {
+      if (it == 1)
+        st.diag.push_back(1.0 / alpha);
+      else {
+        st.diag.push_back(1.0 / alpha + beta / alpha_old);
+        st.offdiag.push_back(std::sqrt(beta) / alpha_old);
+      }
+    }
+    alpha_old = alpha;
+    rho_old = rho;
+    c = check(it, rn);
+  }
+  st.its = it;
+  st.rn = rn;
+  st.status = c;
+  return st;
+}
+
+// eigenvalues of a symmetric tridiagonal matrix: implicit QL iteration with Wilkinson shifts
+static std::vector<double> tridiag_eigs(std::vector<double> d, std::vector<double> e) {
+  const int n = (int)d.size();
+  e.resize(n, 0.0);
+  for (int l = 0; l < n; ++l) {
+    for (int iter = 0; iter < 100; ++iter) {
+      int m = l;
+      for (; m < n - 1; ++m)
+        if (std::fabs(e[m]) <= 1e-15 * (std::fabs(d[m]) + std::fabs(d[m + 1]))) break;
+      if (m == l) break;
+      double g = (d[l + 1] - d[l]) / (2.0 * e[l]);
+      double r = std::hypot(g, 1.0);
+      g = d[m] - d[l] + e[l] / (g + std::copysign(r, g));
+      double sn = 1, cs = 1, p = 0;
+      bool deflated = false;
+      for (int i = m - 1; i >= l; --i) {
+        double f = sn * e[i], bb = cs * e[i];
+        r = std::hypot(f, g);
+        e[i + 1] = r;
+        if (r == 0.0) {
+          d[i + 1] -= p;
+          e[m] = 0.0;
+          deflated = true;
+          break;
+        }
+        sn = f / r;
+        cs = g / r;
+        g = d[i + 1] - p;
+        r = (d[i] - g) * sn + 2.0 * cs * bb;
+        p = sn * r;
+        d[i + 1] = g + p;
+        g = cs * r - bb;
+      }
+      if (deflated) continue;
+      d[l] -= p;
+      e[l] = g;
+      e[m] = 0.0;
+    }
+  }
+  std::sort(d.begin(), d.end());
+  return d;
+}
+
+// MGLevelInfo list for phMG with the Bisect p-sequence (multigrid_preconditioner_base.cpp:97-323)
+static std::vector<std::pair<std::array<int, 3>, int>> mg_level_list(const int Nf[3], int degree, int min_coarse) {
+  std::vector<std::array<int, 3>> h;
+  std::array<int, 3> Nc = {Nf[0], Nf[1], Nf[2]};
+  h.push_back(Nc);
+  while (Nc[0] % 2 == 0 && Nc[1] % 2 == 0 && Nc[2] % 2 == 0 && Nc[0] / 2 >= min_coarse && Nc[1] / 2 >= min_coarse &&
+         Nc[2] / 2 >= min_coarse) {
+    for (int e = 0; e < 3; ++e) Nc[e] /= 2;
+    h.push_back(Nc);
+  }
+  std::reverse(h.begin(), h.end());
+  std::vector<int> p;
+  int pp = degree;
+  do {
+    p.push_back(pp);
+    pp = std::max(pp / 2, 1);
+  } while (pp != p.back());
+  std::reverse(p.begin(), p.end());
+  std::vector<std::pair<std::array<int, 3>, int>> out;
+  for (size_t i = 0; i + 1 < h.size(); ++i) out.push_back({h[i], p.front()});
+  for (int q : p) out.push_back({h.back(), q});
+  return out;
+}
+}  // namespace exg
+
+// ============================================================================================
+// multigrid
+// ============================================================================================
+template <class T>
+static void level_eigen(MGLevel& L, const exg_mg_desc& d, cudaStream_t s) {
+  // Lanczos estimate of lambda_max(D^-1 A) from CG on A x = b, b_i = (i mod 11) - mean
+  // (deal.II PreconditionChebyshev::estimate_eigenvalues, chebyshev_smoother.h:149-210)
+  long long n = L.n;
+  std::vector<T> hb(n);
+  double mean = 0;
+  for (long long i = 0; i < n; ++i) {
+    hb[i] = (T)(i % 11);
+    mean += (double)hb[i];
+  }
+  mean /= (double)n;
+  for (long long i = 0; i < n; ++i) hb[i] = hb[i] - (T)mean;
+  T* b = (T*)dalloc(n * sizeof(T));
+  T* x = (T*)dalloc(n * sizeof(T));
+  T* r = (T*)dalloc(n * sizeof(T));
+  T* z = (T*)dalloc(n * sizeof(T));
+  T* p = (T*)dalloc(n * sizeof(T));
+  T* v = (T*)dalloc(n * sizeof(T));
+  EXG_CUDA(cudaMemcpyAsync(b, hb.data(), n * sizeof(T), cudaMemcpyHostToDevice, s));
+  EXG_CUDA(cudaMemsetAsync(x, 0, n * sizeof(T), s));
+  Reduction red = Reduction::create();
+  const T* dinv = (const T*)L.invd;
+  auto A = [&](const T* in, T* out) { L.op->apply(in, out, 1, s); };
+  auto P = [&](const T* in, T* out) -> double {
+    precond_dot<T>(dinv, in, out, n, red, 4, s);
+    return read_slot(red, 4, s);
+  };
+  CGStats st = pcg_run<T>(A, P, b, x, n, 0.0, 1e-10, d.eig_iters, true, true, r, z, p, v, red, s);
+  EXG_CUDA(cudaStreamSynchronize(s));
+  red.destroy();
+  for (T* ptr : {b, x, r, z, p, v}) cudaFree(ptr);
+  std::vector<double> ev = tridiag_eigs(st.diag, st.offdiag);
+  L.eig_its = st.its;
+  L.lambda_max = ev.empty() ? 1.0 : ev.back();
+  L.lambda_min = ev.empty() ? 1.0 : ev.front();
+  double lmax = 1.2 * L.lambda_max;
+  double alpha = d.smoothing_range > 1.0 ? lmax / d.smoothing_range : std::min(0.9 * lmax, L.lambda_min);
+  L.delta = (lmax - alpha) * 0.5;
+  L.theta = (lmax + alpha) * 0.5;
+}
+
+static TransferParams make_transfer(const MGLevel& c, const MGLevel& f) {
+  TransferParams P{};
+  P.is_h = c.N[0] != f.N[0];
+  P.nf = f.degree + 1;
+  P.nc = c.degree + 1;
+  for (int e = 0; e < 3; ++e) {
+    P.Nf[e] = f.N[e];
+    P.Nc[e] = c.N[e];
+  }
+  std::vector<double> zc = gauss_lobatto(P.nc), zf = gauss_lobatto(P.nf);
+  if (P.is_h) {
+    for (int ch = 0; ch < 2; ++ch)
+      for (int i = 0; i < P.nf; ++i)
+        for (int j = 0; j < P.nc; ++j) P.P[ch][i * P.nc + j] = lagrange(zc, j, 0.5 * (ch + zf[i]));
+  } else {
+    for (int i = 0; i < P.nf; ++i)
+      for (int j = 0; j < P.nc; ++j) P.P[0][i * P.nc + j] = P.P[1][i * P.nc + j] = lagrange(zc, j, zf[i]);
+  }
+  return P;
+}
+
+exg_mg::exg_mg(const exg_op& fine, const exg_mg_desc& d) : desc(d) {
+  EXG_CHECK(d.mg_precision == EXG_PREC_F32 || d.mg_precision == EXG_PREC_F64, EXG_ERR_INVALID,
+            "mg_precision must be EXG_PREC_F32 or EXG_PREC_F64");
+  EXG_CHECK(d.cheb_degree >= 1 && d.eig_iters >= 1, EXG_ERR_INVALID, "bad smoother parameters");
+  prec = d.mg_precision;
+  coarse_prec = d.coarse_double ? EXG_PREC_F64 : prec;
+  auto list = mg_level_list(fine.mesh.N, fine.degree, std::max(1, d.min_coarse_cells));
+  EXG_CHECK(list.size() <= 32, EXG_ERR_UNSUPPORTED, "too many levels");
+  cudaStream_t s = nullptr;
+  lv.resize(list.size());
+  for (size_t l = 0; l < list.size(); ++l) {
+    MGLevel& L = lv[l];
+    for (int e = 0; e < 3; ++e) L.N[e] = list[l].first[e];
+    L.degree = list[l].second;
+    MeshInfo m = fine.mesh;
+    for (int e = 0; e < 3; ++e) {
+      m.d.n_cells[e] = L.N[e];
+      m.N[e] = L.N[e];
+      m.h[e] = (m.d.hi[e] - m.d.lo[e]) / L.N[e];
+    }
+    L.op.reset(new exg_op(m, L.degree, fine.ip, prec));
+    L.n = L.op->n_dofs();
+    size_t bytes = L.n * psize(prec);
+    L.sol = dalloc(bytes);
+    L.def = dalloc(bytes);
+    L.t = dalloc(bytes);
+    EXG_CUDA(cudaMemset(L.sol, 0, bytes));
+    EXG_CUDA(cudaMemset(L.def, 0, bytes));
+    if (l > 0) {
+      L.tmp = dalloc(bytes);
+      L.old = dalloc(bytes);
+      L.invd = dalloc(bytes);
+      L.op->diagonal(L.invd, true, s);
+      if (prec == EXG_PREC_F32)
+        level_eigen<float>(L, d, s);
+      else
+        level_eigen<double>(L, d, s);
+      L.tr = make_transfer(lv[l - 1], L);
+    } else {
+      n_coarse = (int)L.n;
+      EXG_CHECK(L.n <= 4096, EXG_ERR_UNSUPPORTED, "coarse level too large for the single-CTA coarse solver");
+      MeshInfo mc = m;
+      coarse_op.reset(new exg_op(mc, L.degree, fine.ip, coarse_prec));
+      size_t cb = psize(coarse_prec);
+      coarseA = dalloc((size_t)L.n * L.n * cb);
+      void* eye = dalloc((size_t)L.n * L.n * cb);
+      if (coarse_prec == EXG_PREC_F32)
+        identity<float>((float*)eye, (int)L.n, s);
+      else
+        identity<double>((double*)eye, (int)L.n, s);
+      coarse_op->apply(eye, coarseA, (int)L.n, s);
+      EXG_CUDA(cudaDeviceSynchronize());
+      cudaFree(eye);
+      coarse_invd = dalloc(L.n * cb);
+      coarse_op->diagonal(coarse_invd, true, s);
+      coarse_x = dalloc(L.n * cb);
+      EXG_CUDA(cudaMemset(coarse_x, 0, L.n * cb));
+      its_dev = (long long*)dalloc(sizeof(long long));
+      EXG_CUDA(cudaMemset(its_dev, 0, sizeof(long long)));
+    }
+  }
+  EXG_CUDA(cudaDeviceSynchronize());
+  EXG_CUDA(cudaStreamCreateWithFlags(&cap_stream, cudaStreamNonBlocking));
+}
+
+exg_mg::~exg_mg() {
+  if (graph_exec) cudaGraphExecDestroy(graph_exec);
+  if (graph) cudaGraphDestroy(graph);
+  if (cap_stream) cudaStreamDestroy(cap_stream);
+  for (auto& L : lv)
+    for (void* p : {L.invd, L.sol, L.def, L.t, L.tmp, L.old})
+      if (p) cudaFree(p);
+  for (void* p : {coarseA, coarse_invd, coarse_x, (void*)its_dev})
+    if (p) cudaFree(p);
+}
+
+void exg_mg::smooth(int l, bool zero_start, cudaStream_t s) {
+  MGLevel& L = lv[l];
+  const int deg = desc.cheb_degree;
+  auto upd = [&](int mode, double f1, double f2) {
+    if (prec == EXG_PREC_F32)
+      chebyshev_update<float>(mode, (float*)L.sol, (float*)L.old, (const float*)L.def, (const float*)L.tmp,
+                              (const float*)L.invd, f1, f2, L.n, s);
+    else
+      chebyshev_update<double>(mode, (double*)L.sol, (double*)L.old, (const double*)L.def, (const double*)L.tmp,
+                               (const double*)L.invd, f1, f2, L.n, s);
+  };
+  int first;
+  if (zero_start) {
+    upd(0, 0.0, 1.0 / L.theta);
+    first = 0;
+  } else {
+    L.op->apply(L.sol, L.tmp, 1, s);
+    upd(1, 0.0, 1.0 / L.theta);
+    first = 1;
+  }
+  if (deg < 2 || std::fabs(L.delta) < 1e-40) return;
+  double rhok = L.delta / L.theta, sigma = L.theta / L.delta;
+  for (int k = 0; k < deg - 1; ++k) {
+    L.op->apply(L.sol, L.tmp, 1, s);
+    double rhokp = 1.0 / (2.0 * sigma - rhok);
+    double f1 = rhokp * rhok, f2 = 2.0 * rhokp / L.delta;
+    rhok = rhokp;
+    int idx = k + 1 + first;
+    upd(idx == 1 ? 2 : 3, f1, f2);
+  }
+}
+
+void exg_mg::v_cycle(int l, cudaStream_t s) {
+  MGLevel& L = lv[l];
+  if (l == 0) {
+    if (prec == EXG_PREC_F32 && coarse_prec == EXG_PREC_F32)
+      coarse_cg<float, float>((const float*)coarseA, (const float*)coarse_invd, (const float*)L.def, (float*)L.sol,
+                              (float*)coarse_x, n_coarse, desc.coarse_rel_tol, desc.coarse_abs_tol,
+                              desc.coarse_max_iter, desc.singular, its_dev, s);
+    else if (prec == EXG_PREC_F32)
+      coarse_cg<float, double>((const double*)coarseA, (const double*)coarse_invd, (const float*)L.def,
+                               (float*)L.sol, (double*)coarse_x, n_coarse, desc.coarse_rel_tol, desc.coarse_abs_tol,
+                               desc.coarse_max_iter, desc.singular, its_dev, s);
+    else
+      coarse_cg<double, double>((const double*)coarseA, (const double*)coarse_invd, (const double*)L.def,
+                                (double*)L.sol, (double*)coarse_x, n_coarse, desc.coarse_rel_tol,
+                                desc.coarse_abs_tol, desc.coarse_max_iter, desc.singular, its_dev, s);
+    return;
+  }
+  MGLevel& C = lv[l - 1];
+  smooth(l, true, s);
+  L.op->apply(L.sol, L.t, 1, s);
+  if (prec == EXG_PREC_F32) {
+    rsub<float>((const float*)L.def, (float*)L.t, L.n, s);
+    restrict_add<float>(L.tr, (const float*)L.t, (float*)C.def, s);
+  } else {
+    rsub<double>((const double*)L.def, (double*)L.t, L.n, s);
+    restrict_add<double>(L.tr, (const double*)L.t, (double*)C.def, s);
+  }
+  v_cycle(l - 1, s);
+  if (prec == EXG_PREC_F32)
+    prolongate_add<float>(L.tr, (const float*)C.sol, (float*)L.sol, s);
+  else
+    prolongate_add<double>(L.tr, (const double*)C.sol, (double*)L.sol, s);
+  smooth(l, false, s);
+}
+
+void exg_mg::run_vcycle(cudaStream_t s) {
+  int top = (int)lv.size() - 1;
+  for (int l = 0; l < top; ++l) EXG_CUDA(cudaMemsetAsync(lv[l].def, 0, lv[l].n * psize(prec), s));
+  v_cycle(top, s);
+}
+
+void exg_mg::vmult(const double* src, double* dst, cudaStream_t s) {
+  MGLevel& F = lv.back();
+  vec_copy_convert(src, EXG_PREC_F64, F.def, prec, F.n, s);
+  if (desc.use_graph) {
+    if (!graph_exec) {
+      // capture once on an internal stream (capture is not allowed on the legacy default stream)
+      cudaEvent_t ev;
+      EXG_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+      EXG_CUDA(cudaEventRecord(ev, s));
+      EXG_CUDA(cudaStreamWaitEvent(cap_stream, ev, 0));
+      EXG_CUDA(cudaStreamBeginCapture(cap_stream, cudaStreamCaptureModeThreadLocal));
+      run_vcycle(cap_stream);
+      EXG_CUDA(cudaStreamEndCapture(cap_stream, &graph));
+      EXG_CUDA(cudaGraphInstantiate(&graph_exec, graph, 0));
+      EXG_CUDA(cudaEventDestroy(ev));
+    }
+    EXG_CUDA(cudaGraphLaunch(graph_exec, s));
+  } else {
+    run_vcycle(s);
+  }
+  vec_copy_convert(F.sol, prec, dst, EXG_PREC_F64, F.n, s);
+  ++vcycles;
+}
+
+void exg_mg::info(exg_mg_info& out) const {
+  std::memset(&out, 0, sizeof(out));
+  out.n_levels = (int)lv.size();
+  for (size_t l = 0; l < lv.size(); ++l) {
+    out.degree[l] = lv[l].degree;
+    for (int e = 0; e < 3; ++e) out.n_cells[l][e] = lv[l].N[e];
+    out.lambda_max[l] = lv[l].lambda_max;
+    out.eig_iters[l] = lv[l].eig_its;
+  }
+  long long its = 0;
+  if (its_dev) cudaMemcpy(&its, its_dev, sizeof(long long), cudaMemcpyDeviceToHost);
+  out.coarse_iterations = its;
+  out.vcycles = vcycles;
+}
+
+// ============================================================================================
+// outer CG
+// ============================================================================================
+exg_status exg::cg_solve(exg_op& op, exg_mg* mg, const exg_cg_desc& d, const double* b, double* x, exg_cg_result& res,
+                         cudaStream_t s) {
+  long long n = op.n_dofs();
+  double *r = (double*)dalloc(n * 8), *z = (double*)dalloc(n * 8), *p = (double*)dalloc(n * 8),
+         *v = (double*)dalloc(n * 8);
+  double* dinv = nullptr;
+  Reduction red = Reduction::create();
+  if (d.precond == 1) {
+    dinv = (double*)dalloc(n * 8);
+    op.diagonal(dinv, true, s);
+  }
+  EXG_CUDA(cudaStreamSynchronize(s));
+  auto t0 = std::chrono::steady_clock::now();
+  auto A = [&](const double* in, double* out) { op.apply(in, out, 1, s); };
+  auto P = [&](const double* in, double* out) -> double {
+    if (d.precond == 2) {
+      mg->vmult(in, out, s);
+      dot<double>(in, out, n, red, 4, s);
+    } else {
+      precond_dot<double>(d.precond == 1 ? dinv : nullptr, in, out, n, red, 4, s);
+    }
+    return read_slot(red, 4, s);
+  };
+  CGStats st = pcg_run<double>(A, P, b, x, n, d.rel_tol, d.abs_tol, d.max_iter, false, false, r, z, p, v, red, s);
+  EXG_CUDA(cudaStreamSynchronize(s));
+  auto t1 = std::chrono::steady_clock::now();
+  red.destroy();
+  for (double* ptr : {r, z, p, v, dinv})
+    if (ptr) cudaFree(ptr);
+  res.iterations = st.its;
+  res.converged = st.status == 0;
+  res.r0 = st.r0;
+  res.rn = st.rn;
+  res.rho = st.its > 0 && st.r0 > 0 ? std::pow(st.rn / st.r0, 1.0 / st.its) : 0.0;
+  res.n10 = (res.rho > 0 && res.rho < 1) ? -10.0 * std::log(10.0) / std::log(res.rho) : 0.0;
+  res.seconds = std::chrono::duration<double>(t1 - t0).count();
+  if (st.status == 2) return EXG_ERR_NONFINITE;
+  if (st.status == 1) return EXG_ERR_NOT_CONVERGED;
+  return EXG_OK;
+}

@@ -1,0 +1,91 @@
+// Host-side objects behind the C ABI handles.
+#pragma once
+
+#include <memory>
+#include <vector>
+
+#include "general.h"
+#include "internal.h"
+#include "solver_kernels.h"
+
+struct exg_mesh {
+  exg::MeshInfo info;
+  explicit exg_mesh(const exg::MeshInfo& m) : info(m) {}
+};
+
+namespace exg {
+MeshInfo make_mesh_info(const exg_mesh_desc& d);
+}
+
+// SIPG Laplace operator (Poisson::LaplaceOperator)
+struct exg_op {
+  exg::MeshInfo mesh;
+  int degree, n;
+  double ip;
+  int precision;
+  bool cartesian;
+  exg::FE1D fe;
+  exg::CartHost cart;
+  int cpb = 0;  // Cartesian cells per block (0 = tuned default)
+  std::unique_ptr<exg::GeneralGeom> geo;      // curved meshes
+  std::unique_ptr<exg::GeneralGeom> rhs_geo;  // FP64 geometry with points (rhs / quadrature points)
+
+  exg_op(const exg::MeshInfo& m, int degree, double ip, int precision);
+  long long n_dofs() const { return mesh.n_cells() * n * n * n; }
+  void apply(const void* src, void* dst, int n_rhs, cudaStream_t s) const;
+  void diagonal(void* d, bool invert, cudaStream_t s) const;
+  void quadrature_points(double* cx, double* fx, long long* ncp, long long* nfp, cudaStream_t s);
+  void rhs(const double* f, const double* g, const double* h, double* b, cudaStream_t s);
+  void ensure_rhs_geometry(cudaStream_t s);
+};
+
+namespace exg {
+struct MGLevel {
+  int N[3];
+  int degree;
+  std::unique_ptr<exg_op> op;
+  long long n = 0;
+  void* invd = nullptr;
+  void* sol = nullptr;
+  void* def = nullptr;
+  void* t = nullptr;
+  void* tmp = nullptr;
+  void* old = nullptr;
+  double theta = 1, delta = 0, lambda_max = 0, lambda_min = 0;
+  int eig_its = 0;
+  TransferParams tr{};  // transfer from level l-1 to l
+};
+}  // namespace exg
+
+// multigrid preconditioner (MultigridPreconditionerBase + MultigridAlgorithm)
+struct exg_mg {
+  exg_mg_desc desc;
+  int prec;  // level precision
+  std::vector<exg::MGLevel> lv;
+  int coarse_prec;
+  std::unique_ptr<exg_op> coarse_op;
+  void* coarseA = nullptr;
+  void* coarse_invd = nullptr;
+  void* coarse_x = nullptr;
+  long long* its_dev = nullptr;
+  int n_coarse = 0;
+  cudaStream_t cap_stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t graph_exec = nullptr;
+  long long vcycles = 0;
+
+  exg_mg(const exg_op& fine, const exg_mg_desc& d);
+  ~exg_mg();
+  void vmult(const double* src, double* dst, cudaStream_t s);
+  void info(exg_mg_info& out) const;
+
+ private:
+  void v_cycle(int l, cudaStream_t s);
+  void smooth(int l, bool zero_start, cudaStream_t s);
+  void run_vcycle(cudaStream_t s);
+};
+
+namespace exg {
+exg_status cg_solve(exg_op& op, exg_mg* mg, const exg_cg_desc& d, const double* b, double* x, exg_cg_result& r,
+                    cudaStream_t s);
+}

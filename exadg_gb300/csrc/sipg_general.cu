@@ -1,0 +1,888 @@
+// SIPG Laplace operator on curved (MappingQ) hex meshes, plus the geometry setup, right-hand side,
+// diagonal and quadrature points shared by all meshes.
+//
+// Geometry: the mapping interpolates the chart manifold (DeformedCubeManifold::push_forward,
+// grid/deformed_cube_manifold.h:47-59) at the Gauss-Lobatto support points of degree m in every
+// cell, as MappingQ(m) does with a chart manifold.  A setup kernel evaluates x, J at the cell and
+// face quadrature points (QGauss(k+1)) in FP64 and stores, per cell:
+//   cell  q : G = JxW J^{-1} J^{-T} (6 values)            -- do_cell_integral, laplace_operator.cpp:129-137
+//   face  q : a_own = J_own^{-1} n-, a_nb = J_nb^{-1} n-, JxW-   -- do_face_integral :139-163
+// with n- / JxW- taken from the '-' (interior) side of every face as deal.II's FEFaceEvaluation does.
+//
+// Apply kernel: element-centric; CPB cells per block, one thread per line of a cell for the
+// volume sweeps and one thread per face point for the face terms.  No atomics.
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "df64.cuh"
+#include "general.h"
+#include "internal.h"
+
+namespace exg {
+
+// ------------------------------------------------------------------------------------------------
+// geometry setup (FP64)
+// ------------------------------------------------------------------------------------------------
+struct MapParams {
+  int m1;  // mapping nodes per direction
+  double nodes[12];
+  double gq[10], gw[10];
+  int nq;
+  double lo[3], h[3];
+  double amp, left, right;
+  int freq;
+  int N[3];
+  int periodic[3];
+};
+
+__device__ void push_forward(const MapParams& P, const double X[3], double x[3]) {
+  double s = P.amp;
+  if (s != 0.0)
+    for (int e = 0; e < 3; ++e) s *= sin(P.freq * M_PI * (X[e] - P.left) / (P.right - P.left));
+  for (int e = 0; e < 3; ++e) x[e] = X[e] + s;
+}
+
+__device__ double lag(const double* z, int n, int i, double x) {
+  double v = 1.0;
+  for (int j = 0; j < n; ++j)
+    if (j != i) v *= (x - z[j]) / (z[i] - z[j]);
+  return v;
+}
+__device__ double lag_d(const double* z, int n, int i, double x) {
+  double s = 0.0;
+  for (int m = 0; m < n; ++m) {
+    if (m == i) continue;
+    double t = 1.0 / (z[i] - z[m]);
+    for (int j = 0; j < n; ++j)
+      if (j != i && j != m) t *= (x - z[j]) / (z[i] - z[j]);
+    s += t;
+  }
+  return s;
+}
+
+// x(xi) and J(xi) of cell ci from the interpolated manifold
+__device__ void map_eval(const MapParams& P, const int ci[3], const double xi[3], double x[3], double J[3][3]) {
+  double v[3][12], dv[3][12];
+  for (int e = 0; e < 3; ++e)
+    for (int a = 0; a < P.m1; ++a) {
+      v[e][a] = lag(P.nodes, P.m1, a, xi[e]);
+      dv[e][a] = lag_d(P.nodes, P.m1, a, xi[e]);
+    }
+  for (int e = 0; e < 3; ++e) {
+    x[e] = 0;
+    J[e][0] = J[e][1] = J[e][2] = 0;
+  }
+  for (int k = 0; k < P.m1; ++k)
+    for (int j = 0; j < P.m1; ++j)
+      for (int i = 0; i < P.m1; ++i) {
+        double X[3] = {P.lo[0] + (ci[0] + P.nodes[i]) * P.h[0], P.lo[1] + (ci[1] + P.nodes[j]) * P.h[1],
+                       P.lo[2] + (ci[2] + P.nodes[k]) * P.h[2]};
+        double p[3];
+        push_forward(P, X, p);
+        double w = v[0][i] * v[1][j] * v[2][k];
+        double w0 = dv[0][i] * v[1][j] * v[2][k];
+        double w1 = v[0][i] * dv[1][j] * v[2][k];
+        double w2 = v[0][i] * v[1][j] * dv[2][k];
+        for (int e = 0; e < 3; ++e) {
+          x[e] += w * p[e];
+          J[e][0] += w0 * p[e];
+          J[e][1] += w1 * p[e];
+          J[e][2] += w2 * p[e];
+        }
+      }
+}
+
+__device__ double inv3(const double J[3][3], double Ji[3][3]) {
+  double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1]) - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0]) +
+               J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+  double id = 1.0 / det;
+  Ji[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) * id;
+  Ji[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+  Ji[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+  Ji[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) * id;
+  Ji[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+  Ji[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+  Ji[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) * id;
+  Ji[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+  Ji[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+  return det;
+}
+
+__device__ __forceinline__ void tang(int d, int& t1, int& t2) {
+  t1 = d == 0 ? 1 : 0;
+  t2 = d == 2 ? 1 : 2;
+}
+
+__device__ __forceinline__ void coords3(const int N[3], long long c, int ci[3]) {
+  ci[0] = (int)(c % N[0]);
+  long long r = c / N[0];
+  ci[1] = (int)(r % N[1]);
+  ci[2] = (int)(r / N[1]);
+}
+
+__device__ long long neighbor_of(const MapParams& P, long long c, int f) {
+  int ci[3];
+  coords3(P.N, c, ci);
+  int d = f / 2, side = f % 2;
+  ci[d] += side ? 1 : -1;
+  if (ci[d] < 0 || ci[d] >= P.N[d]) {
+    if (!P.periodic[d]) return -1;
+    ci[d] = (ci[d] + P.N[d]) % P.N[d];
+  }
+  return ci[0] + (long long)P.N[0] * (ci[1] + (long long)P.N[1] * ci[2]);
+}
+
+// raw data per point: cell q -> [G(6), JxW, x(3)]; face q -> [Jinv(9), n(3), JxW, x(3)]
+__global__ void geom_raw_kernel(MapParams P, long long n_cells, double* __restrict__ cell_raw,
+                                double* __restrict__ face_raw) {
+  const int nq = P.nq, nq3 = nq * nq * nq, nq2 = nq * nq, per = nq3 + 6 * nq2;
+  long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_cells * per) return;
+  long long c = g / per;
+  int p = (int)(g - c * per);
+  int ci[3];
+  coords3(P.N, c, ci);
+  double xi[3], x[3], J[3][3], Ji[3][3];
+  if (p < nq3) {
+    int q0 = p % nq, q1 = (p / nq) % nq, q2 = p / nq2;
+    xi[0] = P.gq[q0];
+    xi[1] = P.gq[q1];
+    xi[2] = P.gq[q2];
+    map_eval(P, ci, xi, x, J);
+    double det = inv3(J, Ji);
+    double JxW = fabs(det) * P.gw[q0] * P.gw[q1] * P.gw[q2];
+    double* o = cell_raw + (c * nq3 + p) * 10;
+    int k = 0;
+    for (int a = 0; a < 3; ++a)
+      for (int b = a; b < 3; ++b) {
+        double s = 0;
+        for (int j = 0; j < 3; ++j) s += Ji[a][j] * Ji[b][j];
+        o[k++] = s * JxW;
+      }
+    o[6] = JxW;
+    o[7] = x[0];
+    o[8] = x[1];
+    o[9] = x[2];
+  } else {
+    int r = p - nq3;
+    int f = r / nq2, qq = r - f * nq2;
+    int d = f / 2, side = f % 2, t1, t2;
+    tang(d, t1, t2);
+    int a = qq % nq, b = qq / nq;
+    xi[d] = side;
+    xi[t1] = P.gq[a];
+    xi[t2] = P.gq[b];
+    map_eval(P, ci, xi, x, J);
+    double det = inv3(J, Ji);
+    double sg = side ? 1.0 : -1.0, n[3], nn = 0;
+    for (int j = 0; j < 3; ++j) {
+      n[j] = sg * Ji[d][j];
+      nn += n[j] * n[j];
+    }
+    nn = sqrt(nn);
+    double* o = face_raw + ((c * 6 + f) * nq2 + qq) * 16;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) o[i * 3 + j] = Ji[i][j];
+    for (int j = 0; j < 3; ++j) o[9 + j] = n[j] / nn;
+    o[12] = fabs(det) * nn * P.gw[a] * P.gw[b];
+    o[13] = x[0];
+    o[14] = x[1];
+    o[15] = x[2];
+  }
+}
+
+// penalty per cell: sum_f w_f |f| / |K|  (interior_penalty_parameter.h:45-97)
+__global__ void geom_tau_kernel(MapParams P, long long n_cells, const double* __restrict__ cell_raw,
+                                const double* __restrict__ face_raw, double* __restrict__ tau) {
+  long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n_cells) return;
+  const int nq = P.nq, nq3 = nq * nq * nq, nq2 = nq * nq;
+  double vol = 0, surf = 0;
+  for (int q = 0; q < nq3; ++q) vol += cell_raw[(c * nq3 + q) * 10 + 6];
+  for (int f = 0; f < 6; ++f) {
+    double w = neighbor_of(P, c, f) < 0 ? 1.0 : 0.5;
+    for (int q = 0; q < nq2; ++q) surf += w * face_raw[((c * 6 + f) * nq2 + q) * 16 + 12];
+  }
+  tau[c] = surf / vol;
+}
+
+// final per-cell data in precision T: cell G (6) and face [a_own(3), a_nb(3), JxW] (7), the
+// '-' side supplying n and JxW; face penalty / kind per cell-face
+template <class T>
+__global__ void geom_final_kernel(MapParams P, long long n_cells, double factor, const int* __restrict__ bc,
+                                  const double* __restrict__ cell_raw, const double* __restrict__ face_raw,
+                                  const double* __restrict__ tau, T* __restrict__ cellG, T* __restrict__ face,
+                                  T* __restrict__ ftau, long long* __restrict__ fnb) {
+  const int nq = P.nq, nq3 = nq * nq * nq, nq2 = nq * nq, per = nq3 + 6 * nq2;
+  long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_cells * per) return;
+  long long c = g / per;
+  int p = (int)(g - c * per);
+  if (p < nq3) {
+    const double* r = cell_raw + (c * nq3 + p) * 10;
+    for (int k = 0; k < 6; ++k) cellG[(c * nq3 + p) * 6 + k] = (T)r[k];
+    return;
+  }
+  int rr = p - nq3;
+  int f = rr / nq2, q = rr - f * nq2;
+  int d = f / 2, side = f % 2;
+  long long nb = neighbor_of(P, c, f);
+  const double* ro = face_raw + ((c * 6 + f) * nq2 + q) * 16;
+  const double* rm = ro;
+  const double* rn = nullptr;
+  if (nb >= 0) {
+    rn = face_raw + ((nb * 6 + (2 * d + 1 - side)) * nq2 + q) * 16;
+    if (side == 0) rm = rn;
+  }
+  const double* nrm = rm + 9;
+  T* o = face + ((c * 6 + f) * nq2 + q) * 7;
+  for (int i = 0; i < 3; ++i) {
+    o[i] = (T)(ro[i * 3 + 0] * nrm[0] + ro[i * 3 + 1] * nrm[1] + ro[i * 3 + 2] * nrm[2]);
+    o[3 + i] = rn ? (T)(rn[i * 3 + 0] * nrm[0] + rn[i * 3 + 1] * nrm[1] + rn[i * 3 + 2] * nrm[2]) : (T)0;
+  }
+  o[6] = (T)rm[12];
+  if (q == 0) {
+    double t = nb >= 0 ? fmax(tau[c], tau[nb]) * factor : tau[c] * factor;
+    ftau[c * 6 + f] = (T)t;
+    // encoding: >= 0 neighbour cell; -1 Dirichlet; -2 Neumann
+    fnb[c * 6 + f] = nb >= 0 ? nb : (bc[f] == EXG_BC_DIRICHLET ? -1 : -2);
+  }
+}
+
+static MapParams map_params(const MeshInfo& m, const FE1D& fe) {
+  MapParams P{};
+  int md = m.d.mapping_degree < 1 ? 1 : m.d.mapping_degree;
+  EXG_CHECK(md <= 10, EXG_ERR_UNSUPPORTED, "mapping degree must be <= 10");
+  std::vector<double> z = gauss_lobatto(md + 1);
+  P.m1 = md + 1;
+  for (int i = 0; i < P.m1; ++i) P.nodes[i] = z[i];
+  P.nq = fe.nq;
+  for (int i = 0; i < fe.nq; ++i) {
+    P.gq[i] = fe.gq[i];
+    P.gw[i] = fe.gw[i];
+  }
+  for (int e = 0; e < 3; ++e) {
+    P.lo[e] = m.d.lo[e];
+    P.h[e] = m.h[e];
+    P.N[e] = m.N[e];
+    P.periodic[e] = m.d.periodic[e];
+  }
+  P.amp = m.d.deform_amp;
+  P.left = m.d.deform_left;
+  P.right = m.d.deform_right;
+  P.freq = m.d.deform_freq;
+  return P;
+}
+
+GeneralGeom::~GeneralGeom() {
+  for (void* p : {(void*)cellG, (void*)face, (void*)ftau, (void*)fnb, (void*)cell_raw, (void*)face_raw, (void*)tau,
+                  (void*)bc_dev})
+    if (p) cudaFree(p);
+}
+
+void GeneralGeom::build(const MeshInfo& m, const FE1D& fe, double ip, int prec, bool keep_raw, cudaStream_t s) {
+  precision = prec;
+  n_cells = m.n_cells();
+  nq = fe.nq;
+  long long nq3 = (long long)nq * nq * nq, nq2 = (long long)nq * nq, per = nq3 + 6 * nq2;
+  MapParams P = map_params(m, fe);
+  EXG_CUDA(cudaMalloc(&cell_raw, n_cells * nq3 * 10 * sizeof(double)));
+  EXG_CUDA(cudaMalloc(&face_raw, n_cells * 6 * nq2 * 16 * sizeof(double)));
+  EXG_CUDA(cudaMalloc(&tau, n_cells * sizeof(double)));
+  EXG_CUDA(cudaMalloc(&bc_dev, 6 * sizeof(int)));
+  EXG_CUDA(cudaMemcpyAsync(bc_dev, m.d.bc, 6 * sizeof(int), cudaMemcpyHostToDevice, s));
+  long long total = n_cells * per;
+  geom_raw_kernel<<<(unsigned)((total + 127) / 128), 128, 0, s>>>(P, n_cells, cell_raw, face_raw);
+  EXG_CUDA(cudaGetLastError());
+  geom_tau_kernel<<<(unsigned)((n_cells + 127) / 128), 128, 0, s>>>(P, n_cells, cell_raw, face_raw, tau);
+  EXG_CUDA(cudaGetLastError());
+  size_t ts = prec == EXG_PREC_F32 ? sizeof(float) : sizeof(double);
+  EXG_CUDA(cudaMalloc(&cellG, n_cells * nq3 * 6 * ts));
+  EXG_CUDA(cudaMalloc(&face, n_cells * 6 * nq2 * 7 * ts));
+  EXG_CUDA(cudaMalloc(&ftau, n_cells * 6 * ts));
+  EXG_CUDA(cudaMalloc(&fnb, n_cells * 6 * sizeof(long long)));
+  double factor = ip * (fe.k + 1.0) * (fe.k + 1.0);
+  if (prec == EXG_PREC_F32)
+    geom_final_kernel<float><<<(unsigned)((total + 127) / 128), 128, 0, s>>>(
+        P, n_cells, factor, bc_dev, cell_raw, face_raw, tau, (float*)cellG, (float*)face, (float*)ftau, fnb);
+  else
+    geom_final_kernel<double><<<(unsigned)((total + 127) / 128), 128, 0, s>>>(
+        P, n_cells, factor, bc_dev, cell_raw, face_raw, tau, (double*)cellG, (double*)face, (double*)ftau, fnb);
+  EXG_CUDA(cudaGetLastError());
+  if (!keep_raw) {
+    EXG_CUDA(cudaStreamSynchronize(s));
+    cudaFree(cell_raw);
+    cudaFree(face_raw);
+    cell_raw = face_raw = nullptr;
+  }
+}
+
+// ------------------------------------------------------------------------------------------------
+// apply kernel
+// ------------------------------------------------------------------------------------------------
+template <int N, class C>
+struct GenCoef {
+  C S[N * N], D[N * N];  // S[q*N + i] = l_i(x_q)
+  C d0[N], d1[N];        // l_i'(0), l_i'(1)
+};
+
+template <int D, int N>
+__device__ __forceinline__ int lidx(int i, int a, int b) {
+  return D == 0 ? i + N * (a + N * b) : (D == 1 ? a + N * (i + N * b) : a + N * (b + N * i));
+}
+
+// index of the face point (p1, p2) on the face normal to d, at position i along d
+__device__ __forceinline__ int fidx(int N, int d, int i, int p1, int p2) {
+  return d == 0 ? i + N * (p1 + N * p2) : (d == 1 ? p1 + N * (i + N * p2) : p1 + N * (p2 + N * i));
+}
+
+template <int N, int CPB, class T>
+__global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restrict__ src, T* __restrict__ dst,
+                                                              const __grid_constant__ GenCoef<N, T> P,
+                                                              const T* __restrict__ cellG, const T* __restrict__ face,
+                                                              const T* __restrict__ ftau,
+                                                              const long long* __restrict__ fnb, long long n_cells,
+                                                              long long n_dofs) {
+  constexpr int N2 = N * N, N3 = N2 * N, NT = CPB * N2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* su = reinterpret_cast<T*>(smem_raw);
+  T* so = su + CPB * N3;
+  T* t0 = so + CPB * N3;
+  T* t1 = t0 + CPB * N3;
+  T* t2 = t1 + CPB * N3;
+  T* fsh = t2 + CPB * N3;  // CPB * 16 * N2 face scratch
+
+  const long long c0 = (long long)blockIdx.x * CPB;
+  const T* s = src + (long long)blockIdx.y * n_dofs;
+  T* o = dst + (long long)blockIdx.y * n_dofs;
+  const int tid = threadIdx.x;
+  const long long base = c0 * N3;
+  const long long nch = min((long long)CPB, n_cells - c0);
+  const int nd = (int)(nch * N3);
+  for (int i = tid; i < CPB * N3; i += NT) {
+    su[i] = i < nd ? s[base + i] : T(0);
+    so[i] = T(0);
+  }
+  __syncthreads();
+  const int lc = tid / N2, l = tid - lc * N2, a = l % N, b = l / N;
+  const bool active = lc < nch;
+  const long long c = c0 + lc;
+  const int co = lc * N3;
+  T* U = su + co;
+  T* A0 = t0 + co;
+  T* A1 = t1 + co;
+  T* A2 = t2 + co;
+  // ---- cell term: gradients at q (x, then y, then z), G, transpose back
+  if (active) {  // x-lines (j=a, k=b)
+    T u[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) u[i] = U[lidx<0, N>(i, a, b)];
+#pragma unroll
+    for (int q = 0; q < N; ++q) {
+      T vs = 0, vd = 0;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        vs = fma(P.S[q * N + i], u[i], vs);
+        vd = fma(P.D[q * N + i], u[i], vd);
+      }
+      A0[lidx<0, N>(q, a, b)] = vs;  // A = S_x u
+      A1[lidx<0, N>(q, a, b)] = vd;  // B = D_x u
+    }
+  }
+  __syncthreads();
+  if (active) {  // y-lines (i=a, k=b): C = S_y A, E = D_y A, F = S_y B
+    T va[N], vb[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      va[i] = A0[lidx<1, N>(i, a, b)];
+      vb[i] = A1[lidx<1, N>(i, a, b)];
+    }
+#pragma unroll
+    for (int q = 0; q < N; ++q) {
+      T cs = 0, ce = 0, cf = 0;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        cs = fma(P.S[q * N + i], va[i], cs);
+        ce = fma(P.D[q * N + i], va[i], ce);
+        cf = fma(P.S[q * N + i], vb[i], cf);
+      }
+      A0[lidx<1, N>(q, a, b)] = cs;
+      A1[lidx<1, N>(q, a, b)] = ce;
+      A2[lidx<1, N>(q, a, b)] = cf;
+    }
+  }
+  __syncthreads();
+  if (active) {  // z-lines (i=a, j=b): g2 = D_z C, g1 = S_z E, g0 = S_z F; flux; transpose
+    T vc[N], ve[N], vf[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      vc[i] = A0[lidx<2, N>(i, a, b)];
+      ve[i] = A1[lidx<2, N>(i, a, b)];
+      vf[i] = A2[lidx<2, N>(i, a, b)];
+    }
+    T f0[N], f1[N], f2[N];
+#pragma unroll
+    for (int q = 0; q < N; ++q) {
+      T g0 = 0, g1 = 0, g2 = 0;
+#pragma unroll
+      for (int i = 0; i < N; ++i) {
+        g0 = fma(P.S[q * N + i], vf[i], g0);
+        g1 = fma(P.S[q * N + i], ve[i], g1);
+        g2 = fma(P.D[q * N + i], vc[i], g2);
+      }
+      const T* G = cellG + (c * N3 + lidx<2, N>(q, a, b)) * 6;
+      T G00 = G[0], G01 = G[1], G02 = G[2], G11 = G[3], G12 = G[4], G22 = G[5];
+      f0[q] = G00 * g0 + G01 * g1 + G02 * g2;
+      f1[q] = G01 * g0 + G11 * g1 + G12 * g2;
+      f2[q] = G02 * g0 + G12 * g1 + G22 * g2;
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      T xf = 0, xe = 0, xc = 0;
+#pragma unroll
+      for (int q = 0; q < N; ++q) {
+        xf = fma(P.S[q * N + i], f0[q], xf);
+        xe = fma(P.S[q * N + i], f1[q], xe);
+        xc = fma(P.D[q * N + i], f2[q], xc);
+      }
+      A2[lidx<2, N>(i, a, b)] = xf;  // F'
+      A1[lidx<2, N>(i, a, b)] = xe;  // E'
+      A0[lidx<2, N>(i, a, b)] = xc;  // C'
+    }
+  }
+  __syncthreads();
+  if (active) {  // y-lines: A' = S^T C' + D^T E', B' = S^T F'
+    T vc[N], ve[N], vf[N];
+#pragma unroll
+    for (int q = 0; q < N; ++q) {
+      vc[q] = A0[lidx<1, N>(q, a, b)];
+      ve[q] = A1[lidx<1, N>(q, a, b)];
+      vf[q] = A2[lidx<1, N>(q, a, b)];
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      T xa = 0, xb = 0;
+#pragma unroll
+      for (int q = 0; q < N; ++q) {
+        xa = fma(P.S[q * N + i], vc[q], xa);
+        xa = fma(P.D[q * N + i], ve[q], xa);
+        xb = fma(P.S[q * N + i], vf[q], xb);
+      }
+      A0[lidx<1, N>(i, a, b)] = xa;
+      A1[lidx<1, N>(i, a, b)] = xb;
+    }
+  }
+  __syncthreads();
+  if (active) {  // x-lines: out = S^T A' + D^T B'
+    T va[N], vb[N];
+#pragma unroll
+    for (int q = 0; q < N; ++q) {
+      va[q] = A0[lidx<0, N>(q, a, b)];
+      vb[q] = A1[lidx<0, N>(q, a, b)];
+    }
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      T x = 0;
+#pragma unroll
+      for (int q = 0; q < N; ++q) {
+        x = fma(P.S[q * N + i], va[q], x);
+        x = fma(P.D[q * N + i], vb[q], x);
+      }
+      so[co + lidx<0, N>(i, a, b)] = x;
+    }
+  }
+  __syncthreads();
+  // ---- face terms
+  T* F = fsh + lc * 16 * N2;
+  T* fv = F;            // own trace value at face nodes
+  T* fn = F + N2;       // own normal-direction derivative at face nodes
+  T* gv = F + 2 * N2;   // neighbour trace value
+  T* gn = F + 3 * N2;   // neighbour normal derivative
+  T* r0 = F + 4 * N2;   // stage-1 buffers (q1, p2)
+  T* r1 = F + 5 * N2;
+  T* r2 = F + 6 * N2;
+  T* r3 = F + 7 * N2;
+  T* r4 = F + 8 * N2;
+  T* r5 = F + 9 * N2;
+  T* cv = F + 10 * N2;  // flux coefficients at face q
+  T* c0_ = F + 11 * N2;
+  T* c1_ = F + 12 * N2;
+  T* c2_ = F + 13 * N2;
+  const int p1 = a, p2 = b;  // this thread's face point / node
+#pragma unroll 1
+  for (int f = 0; f < 6; ++f) {
+    const int d = f >> 1, side = f & 1;
+    int t1d, t2d;
+    tang(d, t1d, t2d);
+    long long nb = active ? fnb[c * 6 + f] : -2;
+    const bool interior = nb >= 0;
+    const T* dside = side ? P.d1 : P.d0;
+    const T* dopp = side ? P.d0 : P.d1;
+    const int iend = side ? N - 1 : 0, iopp = side ? 0 : N - 1;
+    if (active) {
+      T nd = 0;
+      for (int i = 0; i < N; ++i) nd = fma(dside[i], U[fidx(N, d, i, p1, p2)], nd);
+      fv[p2 * N + p1] = U[fidx(N, d, iend, p1, p2)];
+      fn[p2 * N + p1] = nd;
+      if (interior) {
+        const T* un = s + nb * N3;
+        T ndn = 0;
+        for (int i = 0; i < N; ++i) ndn = fma(dopp[i], un[fidx(N, d, i, p1, p2)], ndn);
+        gv[p2 * N + p1] = un[fidx(N, d, iopp, p1, p2)];
+        gn[p2 * N + p1] = ndn;
+      }
+    }
+    __syncthreads();
+    // stage 1 along t1: thread (q1 = p1, p2): contract over node index p1'
+    if (active && nb != -2) {
+      T sv = 0, sdv = 0, sn = 0, nv = 0, ndv = 0, nn = 0;
+      for (int k = 0; k < N; ++k) {
+        T Sq = P.S[p1 * N + k], Dq = P.D[p1 * N + k];
+        sv = fma(Sq, fv[p2 * N + k], sv);
+        sdv = fma(Dq, fv[p2 * N + k], sdv);
+        sn = fma(Sq, fn[p2 * N + k], sn);
+        if (interior) {
+          nv = fma(Sq, gv[p2 * N + k], nv);
+          ndv = fma(Dq, gv[p2 * N + k], ndv);
+          nn = fma(Sq, gn[p2 * N + k], nn);
+        }
+      }
+      r0[p2 * N + p1] = sv;
+      r1[p2 * N + p1] = sdv;
+      r2[p2 * N + p1] = sn;
+      r3[p2 * N + p1] = nv;
+      r4[p2 * N + p1] = ndv;
+      r5[p2 * N + p1] = nn;
+    }
+    __syncthreads();
+    // stage 2 along t2: thread (q1 = p1, q2 = p2): values / reference gradients at the face point,
+    // then the SIPG flux (laplace_operator.cpp:139-163 / 221-265)
+    if (active && nb != -2) {
+      T vo = 0, go_t1 = 0, go_t2 = 0, go_d = 0, vn = 0, gn_t1 = 0, gn_t2 = 0, gn_d = 0;
+      for (int k = 0; k < N; ++k) {
+        T Sq = P.S[p2 * N + k], Dq = P.D[p2 * N + k];
+        vo = fma(Sq, r0[k * N + p1], vo);
+        go_t2 = fma(Dq, r0[k * N + p1], go_t2);
+        go_t1 = fma(Sq, r1[k * N + p1], go_t1);
+        go_d = fma(Sq, r2[k * N + p1], go_d);
+        if (interior) {
+          vn = fma(Sq, r3[k * N + p1], vn);
+          gn_t2 = fma(Dq, r3[k * N + p1], gn_t2);
+          gn_t1 = fma(Sq, r4[k * N + p1], gn_t1);
+          gn_d = fma(Sq, r5[k * N + p1], gn_d);
+        }
+      }
+      const T* fd = face + ((c * 6 + f) * N2 + p2 * N + p1) * 7;
+      T ao[3] = {fd[0], fd[1], fd[2]};
+      T JxW = fd[6];
+      T gref_o[3];
+      gref_o[d] = go_d;
+      gref_o[t1d] = go_t1;
+      gref_o[t2d] = go_t2;
+      T ndo = ao[0] * gref_o[0] + ao[1] * gref_o[1] + ao[2] * gref_o[2];
+      T tau = ftau[c * 6 + f];
+      T gflux, sv;
+      if (interior) {
+        T an[3] = {fd[3], fd[4], fd[5]};
+        T gref_n[3];
+        gref_n[d] = gn_d;
+        gref_n[t1d] = gn_t1;
+        gref_n[t2d] = gn_t2;
+        T ndn = an[0] * gref_n[0] + an[1] * gref_n[1] + an[2] * gref_n[2];
+        const bool own_minus = side == 1;
+        T um = own_minus ? vo : vn, up = own_minus ? vn : vo;
+        T nm = own_minus ? ndo : ndn, np = own_minus ? ndn : ndo;
+        gflux = T(-0.5) * (um - up);
+        T vflux = T(0.5) * (nm + np) - tau * (um - up);
+        sv = own_minus ? -vflux : vflux;
+      } else {  // homogeneous Dirichlet: u+ = -u-, du+/dn = du-/dn
+        gflux = -vo;
+        sv = -(ndo - T(2) * tau * vo);
+      }
+      cv[p2 * N + p1] = JxW * sv;
+      T gj = JxW * gflux;
+      T cc[3] = {gj * ao[0], gj * ao[1], gj * ao[2]};
+      c0_[p2 * N + p1] = cc[d];
+      c1_[p2 * N + p1] = cc[t1d];
+      c2_[p2 * N + p1] = cc[t2d];
+    }
+    __syncthreads();
+    // integrate stage 1 along t2: thread (q1 = p1, node p2)
+    if (active && nb != -2) {
+      T s1 = 0, s2 = 0, s3 = 0, s4 = 0;
+      for (int q = 0; q < N; ++q) {
+        T Sq = P.S[q * N + p2], Dq = P.D[q * N + p2];
+        s1 = fma(Sq, cv[q * N + p1], s1);
+        s2 = fma(Sq, c1_[q * N + p1], s2);
+        s3 = fma(Dq, c2_[q * N + p1], s3);
+        s4 = fma(Sq, c0_[q * N + p1], s4);
+      }
+      r0[p2 * N + p1] = s1;
+      r1[p2 * N + p1] = s2;
+      r2[p2 * N + p1] = s3;
+      r3[p2 * N + p1] = s4;
+    }
+    __syncthreads();
+    // stage 2 along t1: thread (node p1, node p2) owns the line through it along d
+    if (active && nb != -2) {
+      T tv = 0, tn = 0;
+      for (int q = 0; q < N; ++q) {
+        T Sq = P.S[q * N + p1], Dq = P.D[q * N + p1];
+        tv = fma(Sq, r0[p2 * N + q], tv);
+        tv = fma(Dq, r1[p2 * N + q], tv);
+        tv = fma(Sq, r2[p2 * N + q], tv);
+        tn = fma(Sq, r3[p2 * N + q], tn);
+      }
+      so[co + fidx(N, d, iend, p1, p2)] += tv;
+      for (int i = 0; i < N; ++i) so[co + fidx(N, d, i, p1, p2)] += dside[i] * tn;
+    }
+    __syncthreads();
+  }
+  for (int i = tid; i < nd; i += NT) o[base + i] = so[i];
+}
+
+template <int N, class T>
+static GenCoef<N, T> gen_coef(const FE1D& fe) {
+  GenCoef<N, T> P;
+  for (int i = 0; i < N * N; ++i) {
+    P.S[i] = (T)fe.S[i];
+    P.D[i] = (T)fe.D[i];
+  }
+  for (int i = 0; i < N; ++i) {
+    P.d0[i] = (T)fe.dL[i];
+    P.d1[i] = (T)fe.dR[i];
+  }
+  return P;
+}
+
+template <int N>
+constexpr int gen_cpb() {
+  return N <= 3 ? 16 : (N <= 5 ? 8 : (N <= 7 ? 4 : 2));
+}
+
+template <int N, class T>
+static void gen_apply_n(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s) {
+  constexpr int CPB = gen_cpb<N>(), N3 = N * N * N, N2 = N * N;
+  GenCoef<N, T> P = gen_coef<N, T>(fe);
+  size_t smem = (5 * (size_t)CPB * N3 + (size_t)CPB * 16 * N2) * sizeof(T);
+  auto kern = gen_apply_kernel<N, CPB, T>;
+  static bool attr_set = false;
+  if (!attr_set) {
+    EXG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_set = true;
+  }
+  long long blocks = (g.n_cells + CPB - 1) / CPB;
+  dim3 grid((unsigned)blocks, (unsigned)n_rhs);
+  kern<<<grid, CPB * N2, smem, s>>>((const T*)src, (T*)dst, P, (const T*)g.cellG, (const T*)g.face, (const T*)g.ftau,
+                                    g.fnb, g.n_cells, g.n_cells * N3);
+  EXG_CUDA(cudaGetLastError());
+}
+
+template <class T>
+static void gen_apply_t(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s) {
+  switch (fe.n) {
+    case 2: gen_apply_n<2, T>(g, fe, src, dst, n_rhs, s); break;
+    case 3: gen_apply_n<3, T>(g, fe, src, dst, n_rhs, s); break;
+    case 4: gen_apply_n<4, T>(g, fe, src, dst, n_rhs, s); break;
+    case 5: gen_apply_n<5, T>(g, fe, src, dst, n_rhs, s); break;
+    case 6: gen_apply_n<6, T>(g, fe, src, dst, n_rhs, s); break;
+    case 7: gen_apply_n<7, T>(g, fe, src, dst, n_rhs, s); break;
+    case 8: gen_apply_n<8, T>(g, fe, src, dst, n_rhs, s); break;
+    case 9: gen_apply_n<9, T>(g, fe, src, dst, n_rhs, s); break;
+    default: throw Error{EXG_ERR_UNSUPPORTED, "degree must be 1..8"};
+  }
+}
+
+void general_apply(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s) {
+  EXG_CHECK(n_rhs >= 1 && n_rhs <= 65535, EXG_ERR_INVALID, "n_rhs out of range");
+  if (g.precision == EXG_PREC_F32)
+    gen_apply_t<float>(g, fe, src, dst, n_rhs, s);
+  else
+    gen_apply_t<double>(g, fe, src, dst, n_rhs, s);
+}
+
+// ------------------------------------------------------------------------------------------------
+// diagonal (thread per DoF), rhs (thread per DoF), quadrature points
+// ------------------------------------------------------------------------------------------------
+struct FETab {
+  int n;
+  double S[100], D[100], d0[10], d1[10];
+};
+
+template <class T>
+__global__ void gen_diag_kernel(FETab F, const T* __restrict__ cellG, const T* __restrict__ face,
+                                const T* __restrict__ ftau, const long long* __restrict__ fnb, long long n_dofs,
+                                T* __restrict__ out, bool invert) {
+  const int n = F.n, n2 = n * n, n3 = n2 * n;
+  long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_dofs) return;
+  long long c = g / n3;
+  int loc = (int)(g - c * n3);
+  int ix[3] = {loc % n, (loc / n) % n, loc / n2};
+  double sum = 0;
+  for (int q2 = 0; q2 < n; ++q2)
+    for (int q1 = 0; q1 < n; ++q1)
+      for (int q0 = 0; q0 < n; ++q0) {
+        int qs[3] = {q0, q1, q2};
+        double gr[3];
+        for (int k = 0; k < 3; ++k) {
+          double v = 1;
+          for (int e = 0; e < 3; ++e) v *= (e == k ? F.D : F.S)[qs[e] * n + ix[e]];
+          gr[k] = v;
+        }
+        const T* G = cellG + (c * n3 + (q2 * n + q1) * n + q0) * 6;
+        double G00 = G[0], G01 = G[1], G02 = G[2], G11 = G[3], G12 = G[4], G22 = G[5];
+        sum += gr[0] * (G00 * gr[0] + G01 * gr[1] + G02 * gr[2]) + gr[1] * (G01 * gr[0] + G11 * gr[1] + G12 * gr[2]) +
+               gr[2] * (G02 * gr[0] + G12 * gr[1] + G22 * gr[2]);
+      }
+  for (int f = 0; f < 6; ++f) {
+    int d = f / 2, side = f % 2, t1, t2;
+    tang(d, t1, t2);
+    int iend = side ? n - 1 : 0;
+    if (ix[d] != iend) continue;  // GL basis: only face nodes have a trace on the face
+    long long nb = fnb[c * 6 + f];
+    if (nb == -2) continue;  // Neumann
+    double tau = ftau[c * 6 + f];
+    const double* dside = side ? F.d1 : F.d0;
+    for (int q2 = 0; q2 < n; ++q2)
+      for (int q1 = 0; q1 < n; ++q1) {
+        const T* fd = face + ((c * 6 + f) * n2 + q2 * n + q1) * 7;
+        double v = F.S[q1 * n + ix[t1]] * F.S[q2 * n + ix[t2]];
+        double gr[3];
+        gr[d] = dside[ix[d]] * F.S[q1 * n + ix[t1]] * F.S[q2 * n + ix[t2]];
+        gr[t1] = F.D[q1 * n + ix[t1]] * F.S[q2 * n + ix[t2]];
+        gr[t2] = F.S[q1 * n + ix[t1]] * F.D[q2 * n + ix[t2]];
+        double nd = fd[0] * gr[0] + fd[1] * gr[1] + fd[2] * gr[2];
+        double JxW = fd[6];
+        if (nb >= 0) {
+          double s = side == 1 ? -1.0 : 1.0;
+          sum += JxW * (s * v * nd + tau * v * v);
+        } else {
+          sum += JxW * (-2.0 * v * nd + 2.0 * tau * v * v);
+        }
+      }
+  }
+  T r = (T)sum;
+  if (invert) r = fabs((double)r) > 1e-10 ? (T)1 / r : (T)1;
+  out[g] = r;
+}
+
+// b_i = (f, phi_i) - inhomogeneous boundary part, FP64
+__global__ void gen_rhs_kernel(FETab F, const double* __restrict__ cell_raw, const double* __restrict__ face,
+                               const double* __restrict__ ftau, const long long* __restrict__ fnb,
+                               const double* __restrict__ fq, const double* __restrict__ gq,
+                               const double* __restrict__ hq, long long n_dofs, double* __restrict__ b) {
+  const int n = F.n, n2 = n * n, n3 = n2 * n;
+  long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= n_dofs) return;
+  long long c = g / n3;
+  int loc = (int)(g - c * n3);
+  int ix[3] = {loc % n, (loc / n) % n, loc / n2};
+  double sum = 0;
+  if (fq)
+    for (int q2 = 0; q2 < n; ++q2)
+      for (int q1 = 0; q1 < n; ++q1)
+        for (int q0 = 0; q0 < n; ++q0) {
+          long long qi = c * n3 + (q2 * n + q1) * n + q0;
+          double phi = F.S[q0 * n + ix[0]] * F.S[q1 * n + ix[1]] * F.S[q2 * n + ix[2]];
+          sum += fq[qi] * cell_raw[qi * 10 + 6] * phi;
+        }
+  for (int f = 0; f < 6; ++f) {
+    long long nb = fnb[c * 6 + f];
+    if (nb >= 0) continue;
+    int d = f / 2, side = f % 2, t1, t2;
+    tang(d, t1, t2);
+    const double* dside = side ? F.d1 : F.d0;
+    int iend = side ? n - 1 : 0;
+    double tau = ftau[c * 6 + f];
+    for (int q2 = 0; q2 < n; ++q2)
+      for (int q1 = 0; q1 < n; ++q1) {
+        long long fi = (c * 6 + f) * n2 + q2 * n + q1;
+        const double* fd = face + fi * 7;
+        double v = ix[d] == iend ? F.S[q1 * n + ix[t1]] * F.S[q2 * n + ix[t2]] : 0.0;
+        double gr[3];
+        gr[d] = dside[ix[d]] * F.S[q1 * n + ix[t1]] * F.S[q2 * n + ix[t2]];
+        gr[t1] = ix[d] == iend ? F.D[q1 * n + ix[t1]] * F.S[q2 * n + ix[t2]] : 0.0;
+        gr[t2] = ix[d] == iend ? F.S[q1 * n + ix[t1]] * F.D[q2 * n + ix[t2]] : 0.0;
+        double nd = fd[0] * gr[0] + fd[1] * gr[1] + fd[2] * gr[2];
+        double JxW = fd[6];
+        if (nb == -1) {
+          // Dirichlet: phi- = 0, phi+ = 2g: gflux = g, vflux = 2 tau g; rhs -= (g nd - 2 tau g v)
+          double gv = gq ? gq[fi] : 0.0;
+          sum -= JxW * (gv * nd - 2.0 * tau * gv * v);
+        } else {
+          // Neumann: vflux = h; rhs -= (-h v)
+          double hv = hq ? hq[fi] : 0.0;
+          sum += JxW * hv * v;
+        }
+      }
+  }
+  b[g] = sum;
+}
+
+__global__ void gen_points_kernel(const double* __restrict__ cell_raw, const double* __restrict__ face_raw,
+                                  long long n_cell_pts, long long n_face_pts, double* __restrict__ cx,
+                                  double* __restrict__ fx) {
+  long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g < n_cell_pts) {
+    if (cx)
+      for (int e = 0; e < 3; ++e) cx[g * 3 + e] = cell_raw[g * 10 + 7 + e];
+  } else if (g < n_cell_pts + n_face_pts) {
+    long long h = g - n_cell_pts;
+    if (fx)
+      for (int e = 0; e < 3; ++e) fx[h * 3 + e] = face_raw[h * 16 + 13 + e];
+  }
+}
+
+static FETab fetab(const FE1D& fe) {
+  FETab F{};
+  F.n = fe.n;
+  for (int i = 0; i < fe.n * fe.n; ++i) {
+    F.S[i] = fe.S[i];
+    F.D[i] = fe.D[i];
+  }
+  for (int i = 0; i < fe.n; ++i) {
+    F.d0[i] = fe.dL[i];
+    F.d1[i] = fe.dR[i];
+  }
+  return F;
+}
+
+void general_diagonal(const GeneralGeom& g, const FE1D& fe, void* out, bool invert, cudaStream_t s) {
+  long long nd = g.n_cells * fe.n * fe.n * fe.n;
+  FETab F = fetab(fe);
+  if (g.precision == EXG_PREC_F32)
+    gen_diag_kernel<float><<<(unsigned)((nd + 127) / 128), 128, 0, s>>>(F, (const float*)g.cellG, (const float*)g.face,
+                                                                       (const float*)g.ftau, g.fnb, nd, (float*)out,
+                                                                       invert);
+  else
+    gen_diag_kernel<double><<<(unsigned)((nd + 127) / 128), 128, 0, s>>>(
+        F, (const double*)g.cellG, (const double*)g.face, (const double*)g.ftau, g.fnb, nd, (double*)out, invert);
+  EXG_CUDA(cudaGetLastError());
+}
+
+void general_rhs(const GeneralGeom& g, const FE1D& fe, const double* fq, const double* gq, const double* hq, double* b,
+                 cudaStream_t s) {
+  EXG_CHECK(g.precision != EXG_PREC_F32 && g.cell_raw, EXG_ERR_INVALID, "rhs needs FP64 geometry with raw data");
+  long long nd = g.n_cells * fe.n * fe.n * fe.n;
+  FETab F = fetab(fe);
+  gen_rhs_kernel<<<(unsigned)((nd + 127) / 128), 128, 0, s>>>(F, g.cell_raw, (const double*)g.face,
+                                                              (const double*)g.ftau, g.fnb, fq, gq, hq, nd, b);
+  EXG_CUDA(cudaGetLastError());
+}
+
+void general_points(const GeneralGeom& g, double* cx, double* fx, long long* ncp, long long* nfp, cudaStream_t s) {
+  long long nq = g.nq;
+  long long n_cell_pts = g.n_cells * nq * nq * nq, n_face_pts = g.n_cells * 6 * nq * nq;
+  if (ncp) *ncp = n_cell_pts;
+  if (nfp) *nfp = n_face_pts;
+  if (!cx && !fx) return;
+  EXG_CHECK(g.cell_raw, EXG_ERR_INVALID, "geometry built without raw data");
+  long long tot = n_cell_pts + n_face_pts;
+  gen_points_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(g.cell_raw, g.face_raw, n_cell_pts, n_face_pts, cx,
+                                                                  fx);
+  EXG_CUDA(cudaGetLastError());
+}
+
+}  // namespace exg

@@ -1,0 +1,161 @@
+/*
+ * exadg_gb300.h -- C ABI of the GB300-native SIPG Laplace operator, multigrid preconditioner and
+ * CG solver.
+ *
+ * Conventions
+ *   - Every function returns an exg_status (0 = EXG_OK) and never throws across the ABI.
+ *   - Vector pointers are DEVICE pointers owned by the caller; handles are owned by the library.
+ *   - Calls are ordered on the given CUDA stream (a cudaStream_t passed as void*, NULL = default
+ *     stream).  One handle is used by one host thread at a time.
+ *   - DoF ordering: cells lexicographic (x fastest), FE_DGQ(k) nodal values on Gauss-Lobatto
+ *     points lexicographic within a cell (x fastest).
+ *   - apply/vmult overwrite dst (zero_dst = true); src and dst must not alias.
+ *
+ * Each entry point names the ExaDG interface it replaces (paths relative to the ExaDG tree).
+ */
+#ifndef EXADG_GB300_H
+#define EXADG_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int exg_status;
+enum {
+  EXG_OK = 0,
+  EXG_ERR_INVALID = 1,        /* bad argument (size, degree, pointer, descriptor) */
+  EXG_ERR_CUDA = 2,           /* a CUDA call failed */
+  EXG_ERR_NOT_CONVERGED = 3,  /* Krylov solver hit max_iter (deal.II SolverControl::NoConvergence) */
+  EXG_ERR_NONFINITE = 4,      /* NaN / Inf residual (iterative_solvers_dealii_wrapper.h:210-211) */
+  EXG_ERR_UNSUPPORTED = 5,    /* configuration not implemented */
+  EXG_ERR_NEEDS_UPDATE = 6    /* preconditioner used before update() (multigrid_preconditioner_base.cpp:678-680) */
+};
+
+/* arithmetic of an operator instance */
+enum {
+  EXG_PREC_F64 = 0,   /* native FP64 */
+  EXG_PREC_F32 = 1,   /* FP32 (multigrid levels) */
+  EXG_PREC_F64E = 2   /* FP64 storage, FP32-pair ("double-float") arithmetic, ~1e-14 relative */
+};
+
+/* boundary types of the six box sides (x-, x+, y-, y+, z-, z+); ignored on periodic directions */
+enum { EXG_BC_DIRICHLET = 0, EXG_BC_NEUMANN = 1 };
+
+typedef struct {
+  int n_cells[3];       /* cells per direction */
+  double lo[3], hi[3];  /* box corners */
+  int periodic[3];      /* 1 = periodic in that direction */
+  int bc[6];            /* EXG_BC_* per side */
+  double deform_amp;    /* DeformedCubeManifold deformation (grid/deformed_cube_manifold.h:47-59); 0 = affine */
+  int deform_freq;
+  double deform_left, deform_right;
+  int mapping_degree;   /* MappingQ degree used for curvilinear meshes */
+} exg_mesh_desc;
+
+typedef struct exg_mesh exg_mesh;
+typedef struct exg_op exg_op;
+typedef struct exg_mg exg_mg;
+
+/* Structured hex triangulation (replaces GridGenerator::subdivided_hyper_rectangle + manifold
+ * setup, applications/poisson/sine/application.h:181-300; grid/deformed_cube_manifold.h:127-157). */
+exg_status exg_mesh_create(const exg_mesh_desc* desc, exg_mesh** mesh);
+exg_status exg_mesh_destroy(exg_mesh* mesh);
+
+/* SIPG Laplace operator on FE_DGQ(degree), QGauss(degree+1)
+ * (Poisson::LaplaceOperator::initialize, poisson/spatial_discretization/laplace_operator.cpp:33-51;
+ *  penalty IP::calculate_penalty_parameter, operators/interior_penalty_parameter.h:45-97). */
+exg_status exg_sipg_create(const exg_mesh* mesh, int degree, double ip_factor, int precision, exg_op** op);
+exg_status exg_sipg_destroy(exg_op* op);
+exg_status exg_sipg_n_dofs(const exg_op* op, long long* n_dofs);
+exg_status exg_sipg_info(const exg_op* op, int* degree, int* precision, int* cartesian);
+
+/* dst = A src for n_rhs vectors stored back to back (stride n_dofs)
+ * (OperatorBase::vmult / apply, operators/operator_base.cpp:156-168, 264-310;
+ *  Poisson::Operator::vmult, poisson/spatial_discretization/operator.cpp:425-430).
+ * exg_sipg_apply_f64 runs on EXG_PREC_F64 and EXG_PREC_F64E operators, exg_sipg_apply_f32 on
+ * EXG_PREC_F32 operators. */
+exg_status exg_sipg_apply_f64(exg_op* op, const double* src, double* dst, int n_rhs, void* stream);
+exg_status exg_sipg_apply_f32(exg_op* op, const float* src, float* dst, int n_rhs, void* stream);
+
+/* inverse diagonal, |d| <= 1e-10 -> 1
+ * (OperatorBase::calculate_inverse_diagonal, operators/operator_base.cpp:251-262;
+ *  utilities/invert_diagonal.h:35-46) */
+exg_status exg_sipg_inverse_diagonal_f64(exg_op* op, double* d, void* stream);
+exg_status exg_sipg_inverse_diagonal_f32(exg_op* op, float* d, void* stream);
+
+/* Quadrature points where the caller evaluates f, g and h for the right-hand side:
+ * cell points [n_cells][(k+1)^3][3] and boundary-face points [n_cells][6][(k+1)^2][3]
+ * (entries of interior faces are unused). Sizes returned via n_cell_pts / n_face_pts. */
+exg_status exg_sipg_quadrature_points(exg_op* op, double* cell_xyz, double* face_xyz,
+                                      long long* n_cell_pts, long long* n_face_pts, void* stream);
+
+/* b = (f, v) - (inhomogeneous boundary part): Dirichlet g and Neumann h values at the boundary
+ * face points, f at the cell points; any of f/g/h may be NULL (zero)
+ * (Poisson::Operator::rhs, operator.cpp:414-423; OperatorBase::rhs_add, operator_base.cpp:515-554;
+ *  weak_boundary_conditions.h:34-234; RHSOperator, operators/rhs_operator.h). */
+exg_status exg_sipg_rhs(exg_op* op, const double* f_cell, const double* g_face, const double* h_face,
+                        double* b, void* stream);
+
+typedef struct {
+  int mg_precision;        /* EXG_PREC_F32 (reference default MultigridNumber = float) or EXG_PREC_F64 */
+  int cheb_degree;         /* 5 (multigrid_parameters.h:169-217) */
+  double smoothing_range;  /* 20 */
+  int eig_iters;           /* 20 */
+  double coarse_rel_tol;   /* 1e-3 (applications/poisson/sine/application.h:175-177) */
+  double coarse_abs_tol;   /* 1e-12 */
+  int coarse_max_iter;     /* 10000 */
+  int coarse_double;       /* 1: coarse CG in FP64 even when the V-cycle is FP32 */
+  int min_coarse_cells;    /* stop h-coarsening at this many cells per direction (2) */
+  int singular;            /* subtract the mean in the coarse solve (coarse_grid_solvers.h:161-162) */
+  int use_graph;           /* capture the V-cycle as one CUDA graph */
+} exg_mg_desc;
+
+typedef struct {
+  int n_levels;
+  int degree[32];
+  int n_cells[32][3];
+  double lambda_max[32];   /* Lanczos estimate before the 1.2 safety factor */
+  int eig_iters[32];
+  long long coarse_iterations;  /* accumulated coarse CG iterations */
+  long long vcycles;
+} exg_mg_info;
+
+/* phMG (Bisect p-sequence, DG) with Chebyshev-Jacobi smoothing and a coarse CG
+ * (MultigridPreconditionerBase::initialize/vmult, multigrid/multigrid_preconditioner_base.cpp:55-95,
+ *  673-683; MultigridAlgorithm::v_cycle, multigrid/multigrid_algorithm.h:172-240). */
+exg_status exg_mg_default_desc(exg_mg_desc* desc);
+exg_status exg_mg_create(const exg_op* fine, const exg_mg_desc* desc, exg_mg** mg);
+exg_status exg_mg_destroy(exg_mg* mg);
+exg_status exg_mg_vmult(exg_mg* mg, const double* src, double* dst, void* stream);
+exg_status exg_mg_info_get(const exg_mg* mg, exg_mg_info* info);
+
+typedef struct {
+  int max_iter;        /* 10000 */
+  double abs_tol;      /* 1e-20 */
+  double rel_tol;      /* 1e-10 */
+  int precond;         /* 0 none, 1 point Jacobi, 2 multigrid (mg handle) */
+} exg_cg_desc;
+
+typedef struct {
+  int iterations;
+  int converged;
+  double r0, rn;       /* initial / final residual norm */
+  double rho, n10;     /* convergence metrics (iterative_solvers_dealii_wrapper.h:63-78) */
+  double seconds;      /* wall time of the solve (device-synchronised) */
+} exg_cg_result;
+
+/* PCG on A x = b with x as the initial guess (Krylov::KrylovSolver::solve ->
+ * dealii::SolverCG + ReductionControl, solvers/iterative_solvers_dealii_wrapper.h:136-221).
+ * Returns EXG_ERR_NOT_CONVERGED / EXG_ERR_NONFINITE instead of throwing. */
+exg_status exg_cg_default_desc(exg_cg_desc* desc);
+exg_status exg_cg_solve(exg_op* op, exg_mg* mg, const exg_cg_desc* desc, const double* b, double* x,
+                        exg_cg_result* result, void* stream);
+
+const char* exg_status_string(exg_status status);
+const char* exg_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* EXADG_GB300_H */

@@ -1,0 +1,118 @@
+"""GPU parity of the SIPG operator apply against the oracle (C ABI through exadg_gb300).
+
+Tolerances: FP64 and FP64-emulated (FP32-pair) arithmetic <= 1e-12 relative L2, FP32 <= 1e-5."""
+import numpy as np
+import pytest
+
+import exadg_gb300 as E
+import oracle as O
+from tests.gpu_common import pair, rel, require_gpu, to_dev
+from tests.helpers import splitmix_uniform
+
+pytestmark = pytest.mark.gpu
+
+KINDS = ["dirichlet", "mixed", "periodic", "partial_periodic", "anisotropic"]
+
+
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5, 6, 7, 8])
+def test_apply_f64(kind, k):
+    torch = require_gpu()
+    p, m, op = pair(kind, 3, k)
+    x = splitmix_uniform(p.n_dofs, 1)
+    y = op.vmult(op.initialize_dof_vector(), to_dev(torch, x))
+    assert rel(y.cpu().numpy(), p.apply(x)) <= 1e-12
+
+
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("k", [1, 2, 4, 5, 8])
+def test_apply_f64_emulated(kind, k):
+    torch = require_gpu()
+    p, m, op = pair(kind, 3, k, E.PREC_F64E)
+    x = splitmix_uniform(p.n_dofs, 2)
+    y = op.vmult(op.initialize_dof_vector(), to_dev(torch, x))
+    assert rel(y.cpu().numpy(), p.apply(x)) <= 1e-12
+
+
+@pytest.mark.parametrize("kind", KINDS)
+@pytest.mark.parametrize("k", [1, 3, 4, 6, 8])
+def test_apply_f32(kind, k):
+    torch = require_gpu()
+    p, m, op = pair(kind, 3, k, E.PREC_F32)
+    x = splitmix_uniform(p.n_dofs, 3).astype(np.float32)
+    y = op.vmult(op.initialize_dof_vector(), to_dev(torch, x, torch.float32))
+    assert rel(y.cpu().numpy(), p.apply(x.astype(np.float64))) <= 1e-5
+
+
+@pytest.mark.parametrize("prec", [E.PREC_F64, E.PREC_F32, E.PREC_F64E])
+@pytest.mark.parametrize("k", [2, 4])
+def test_apply_multi_rhs(prec, k):
+    torch = require_gpu()
+    p, m, op = pair("mixed", 3, k, prec)
+    dt = torch.float32 if prec == E.PREC_F32 else torch.float64
+    X = np.stack([splitmix_uniform(p.n_dofs, s) for s in (1, 2, 3, 4)])
+    Xd = to_dev(torch, X, dt)
+    Y = op.vmult(op.initialize_dof_vector(4), Xd, n_rhs=4)
+    for r in range(4):
+        y1 = op.vmult(op.initialize_dof_vector(), Xd[r].contiguous())
+        assert torch.equal(Y[r], y1)
+        tol = 1e-5 if prec == E.PREC_F32 else 1e-12
+        assert rel(Y[r].cpu().numpy(), p.apply(X[r].astype(np.float32 if prec == E.PREC_F32 else np.float64).astype(np.float64))) <= tol
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5])
+@pytest.mark.parametrize("prec", [E.PREC_F64, E.PREC_F32])
+def test_apply_curved(k, prec):
+    torch = require_gpu()
+    p, m, op = pair("curved", 3, k, prec)
+    assert not op.cartesian
+    dt = torch.float32 if prec == E.PREC_F32 else torch.float64
+    x = splitmix_uniform(p.n_dofs, 5)
+    if prec == E.PREC_F32:
+        x = x.astype(np.float32).astype(np.float64)
+    y = op.vmult(op.initialize_dof_vector(), to_dev(torch, x, dt))
+    assert rel(y.cpu().numpy(), p.apply(x)) <= (1e-5 if prec == E.PREC_F32 else 1e-12)
+
+
+@pytest.mark.parametrize("kind", ["mixed", "periodic", "curved", "anisotropic"])
+@pytest.mark.parametrize("k", [1, 3, 5])
+def test_inverse_diagonal(kind, k):
+    torch = require_gpu()
+    p, m, op = pair(kind, 3, k)
+    d = op.calculate_inverse_diagonal(op.initialize_dof_vector())
+    ref = 1.0 / p.diagonal()
+    assert rel(d.cpu().numpy(), ref) <= 1e-12
+
+
+@pytest.mark.parametrize("curved", [False, True])
+@pytest.mark.parametrize("k", [1, 3, 4])
+def test_rhs_sine(curved, k):
+    torch = require_gpu()
+    p, m, op = pair("curved" if curved else "mixed", 3, k)
+    cx, fx = op.quadrature_points()
+    w = 3 * np.pi
+
+    def u(x):
+        return torch.sin(w * x[:, 0]) * torch.sin(w * x[:, 1]) * torch.sin(w * x[:, 2])
+
+    f = 3 * w * w * u(cx)
+    g = u(fx)
+    h = w * torch.cos(w * fx[:, 0]) * torch.sin(w * fx[:, 1]) * torch.sin(w * fx[:, 2])
+    b = op.rhs(f.contiguous(), g.contiguous(), h.contiguous())
+    ref = p.rhs(O.FN_SINE, w)
+    assert rel(b.cpu().numpy(), ref) <= 1e-12
+
+
+def test_apply_large_mesh_properties():
+    # full-size property checks (k = 4, 64^3 would need the full oracle): linearity and symmetry
+    torch = require_gpu()
+    m = E.Mesh(24)
+    op = E.LaplaceOperator(m, 4)
+    a = to_dev(torch, splitmix_uniform(op.n_dofs, 11))
+    b = to_dev(torch, splitmix_uniform(op.n_dofs, 12))
+    Aa = op.vmult(op.initialize_dof_vector(), a)
+    Ab = op.vmult(op.initialize_dof_vector(), b)
+    Aab = op.vmult(op.initialize_dof_vector(), (2.0 * a + b).contiguous())
+    assert torch.linalg.norm(Aab - 2.0 * Aa - Ab) <= 1e-12 * torch.linalg.norm(Aab)
+    assert abs(float(a @ Ab - b @ Aa)) <= 1e-12 * float(torch.linalg.norm(a) * torch.linalg.norm(Ab))
+    assert float(a @ Aa) > 0

@@ -1,0 +1,101 @@
+"""GPU parity of the diagonal-preconditioned and multigrid-preconditioned CG against the oracle:
+iteration counts within +-1, Chebyshev eigenvalue estimates, V-cycle output, and the reference's
+sine golden errors reproduced by the GPU solve."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import exadg_gb300 as E
+import oracle as O
+from tests.gpu_common import rel, require_gpu, to_dev
+from tests.helpers import splitmix_uniform
+
+pytestmark = pytest.mark.gpu
+
+GOLD = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "sine_errors.json")))
+
+
+def sine(k, curved, n=8):
+    kw = dict(n_cells=(n, n, n), lo=(-1, -1, -1), hi=(1, 1, 1), bc=(0, 1, 0, 0, 0, 0),
+              deform_amp=0.15 if curved else 0.0, deform_freq=2, deform_left=-1.0, deform_right=1.0,
+              mapping_degree=3)
+    return O.Problem(O.mesh_desc(**kw), k), E.Mesh(**kw)
+
+
+def test_cg_jacobi_config_1():
+    torch = require_gpu()
+    kw = dict(n_cells=(8, 8, 8))
+    p = O.Problem(O.mesh_desc(**kw), 3)
+    op = E.LaplaceOperator(E.Mesh(**kw), 3)
+    b = p.rhs(O.FN_SINE, np.pi)
+    xo, ro = p.solve(b, precond=1)
+    x = op.initialize_dof_vector()
+    solver = E.KrylovSolver(op, None, precond=E.KrylovSolver.JACOBI)
+    its = solver.solve(x, to_dev(torch, b))
+    assert abs(its - ro.iterations) <= 1
+    assert rel(x.cpu().numpy(), xo) <= 1e-8
+
+
+@pytest.mark.parametrize("mg_prec", [E.PREC_F64, E.PREC_F32])
+def test_mg_levels_and_eigenvalues(mg_prec):
+    torch = require_gpu()
+    p, m = sine(4, False)
+    op = E.LaplaceOperator(m, 4)
+    mg = E.MultigridPreconditioner(op, mg_precision=mg_prec)
+    omg = O.Multigrid(p, mg_float=1 if mg_prec == E.PREC_F32 else 0)
+    info = mg.info()
+    ol = omg.levels()
+    assert info["n_levels"] == len(ol)
+    for g, o in zip(info["levels"], ol):
+        assert g["degree"] == o["degree"] and g["n_cells"] == o["n_cells"]
+        if o["eig_iters"]:
+            assert g["eig_iters"] == o["eig_iters"]
+            assert g["lambda_max"] == pytest.approx(o["lambda_max"], rel=1e-9 if mg_prec == E.PREC_F64 else 1e-4)
+
+
+def test_vcycle_matches_oracle_double():
+    torch = require_gpu()
+    p, m = sine(3, True)
+    op = E.LaplaceOperator(m, 3)
+    mg = E.MultigridPreconditioner(op, mg_precision=E.PREC_F64)
+    omg = O.Multigrid(p, mg_float=0)
+    for seed in (1, 2):
+        r = splitmix_uniform(p.n_dofs, seed)
+        z = mg.vmult(op.initialize_dof_vector(), to_dev(torch, r))
+        assert rel(z.cpu().numpy(), omg.vmult(r)) <= 1e-9
+
+
+@pytest.mark.parametrize("curved", [False, True])
+@pytest.mark.parametrize("k", [2, 4, 5])
+@pytest.mark.parametrize("mg_prec", [E.PREC_F64, E.PREC_F32])
+def test_sine_solve_golden_and_iterations(curved, k, mg_prec):
+    torch = require_gpu()
+    p, m = sine(k, curved)
+    op = E.LaplaceOperator(m, k)
+    mg = E.MultigridPreconditioner(op, mg_precision=mg_prec)
+    b = p.rhs(O.FN_SINE, 3 * np.pi)
+    x = op.initialize_dof_vector()
+    solver = E.KrylovSolver(op, mg)
+    its = solver.solve(x, to_dev(torch, b))
+    xo, ro = O.Multigrid(p, mg_float=1 if mg_prec == E.PREC_F32 else 0).solve(b)
+    assert abs(its - ro.iterations) <= 1, (its, ro.iterations)
+    err = p.error(x.cpu().numpy(), O.FN_SINE, 3 * np.pi)
+    gold = GOLD["curvilinear" if curved else "cartesian"]["relative_l2_error"][k - 1]
+    assert abs(err - gold) <= 5e-6 * gold
+
+
+def test_cg_reports_nonfinite_and_max_iter():
+    torch = require_gpu()
+    op = E.LaplaceOperator(E.Mesh(4), 2)
+    b = to_dev(torch, splitmix_uniform(op.n_dofs, 1))
+    x = op.initialize_dof_vector()
+    s = E.KrylovSolver(op, None, precond=E.KrylovSolver.JACOBI, max_iter=2)
+    s.solve(x, b, raise_on_failure=False)
+    assert s.result["status"] == E.EXG_ERR_NOT_CONVERGED and s.result["iterations"] == 2
+    b[5] = float("nan")
+    x.zero_()
+    s2 = E.KrylovSolver(op, None, precond=E.KrylovSolver.JACOBI)
+    s2.solve(x, b, raise_on_failure=False)
+    assert s2.result["status"] == E.EXG_ERR_NONFINITE

@@ -154,8 +154,8 @@ def run_gpu(args):
     B.build()
     E.load_library()
     prec = {"f64": E.PREC_F64, "f32": E.PREC_F32, "f64e": E.PREC_F64E}[args.precision]
-    mesh = E.Mesh(N_CELLS)
-    op = E.LaplaceOperator(mesh, DEGREE, 1.0, prec)
+    mesh = E.Mesh(args.n_cells)
+    op = E.LaplaceOperator(mesh, args.degree, 1.0, prec)
     n = op.n_dofs
     dt = op.dtype
     esize = 4 if prec == E.PREC_F32 else 8
@@ -219,8 +219,9 @@ def run_gpu(args):
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": {"f64": "f64", "f32": "f32", "f64e": "f64 (FP32-pair arithmetic)"}[args.precision],
             "data": "synthetic",
-            "config": {"workload": "SIPG Laplace apply, Cartesian 64^3 cells of [0,1]^3, all Dirichlet, k=%d" % DEGREE,
-                       "degree": DEGREE, "n_cells": N_CELLS ** 3, "n_dofs": n, "precision": args.precision,
+            "config": {"workload": "SIPG Laplace apply, Cartesian %d^3 cells of [0,1]^3, all Dirichlet, k=%d"
+                                   % (args.n_cells, args.degree),
+                       "degree": args.degree, "n_cells": args.n_cells ** 3, "n_dofs": n, "precision": args.precision,
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": "inputs larger than L2 (src+dst %.0f MB > 129 MB)" % (bytes_per_apply / 1e6)},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
@@ -248,6 +249,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--precision", default="f64", choices=["f64", "f32", "f64e"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--n-cells", type=int, default=N_CELLS, help="cells per direction (profiling runs use smaller meshes)")
+    ap.add_argument("--degree", type=int, default=DEGREE)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)

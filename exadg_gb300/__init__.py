@@ -112,7 +112,7 @@ EXPORTED_SYMBOLS = [
     "exg_sipg_info", "exg_sipg_apply_f64", "exg_sipg_apply_f32", "exg_sipg_inverse_diagonal_f64",
     "exg_sipg_inverse_diagonal_f32", "exg_sipg_quadrature_points", "exg_sipg_rhs", "exg_mg_default_desc",
     "exg_mg_create", "exg_mg_destroy", "exg_mg_vmult", "exg_mg_info_get", "exg_cg_default_desc", "exg_cg_solve",
-    "exg_status_string", "exg_last_error",
+    "exg_cg_solve_noalloc", "exg_status_string", "exg_last_error",
 ]
 
 _lib = None
@@ -151,6 +151,7 @@ def load_library(path=LIB_PATH):
         "exg_mg_info_get": [P, ctypes.POINTER(MGInfo)],
         "exg_cg_default_desc": [ctypes.POINTER(CGDesc)],
         "exg_cg_solve": [P, P, ctypes.POINTER(CGDesc), P, P, ctypes.POINTER(CGResult), P],
+        "exg_cg_solve_noalloc": [P, ctypes.POINTER(CGDesc), P, P, ctypes.POINTER(CGResult), P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

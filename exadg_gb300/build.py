@@ -25,6 +25,7 @@ SOURCES = [
     "fe_tables.cpp",
     "host.cpp",
     "capi.cpp",
+    "noalloc.cu",
 ]
 
 

@@ -151,6 +151,18 @@ exg_status exg_cg_default_desc(exg_cg_desc* desc);
 exg_status exg_cg_solve(exg_op* op, exg_mg* mg, const exg_cg_desc* desc, const double* b, double* x,
                         exg_cg_result* result, void* stream);
 
+/* The same point-Jacobi / unpreconditioned CG as exg_cg_solve (desc->precond 0 or 1), but it
+ * allocates nothing: its work vectors live in one statically allocated device array of about
+ * 20 MiB that every GPU loading this library holds until the process exits.  For callers that
+ * cannot call cudaMalloc / cudaFree while they run (a time loop with other streams in flight --
+ * both calls synchronise the device --, a framework whose pool owns the device memory).
+ * Limit: n_dofs <= 524288, otherwise EXG_ERR_INVALID.  The first call on a device looks up the
+ * array's device address (make that first call before any stream capture).  All calls share the
+ * array, so calls that overlap on the GPU race; each call clears what must start at zero.
+ * No counterpart in the reference: an addition of this library. */
+exg_status exg_cg_solve_noalloc(exg_op* op, const exg_cg_desc* desc, const double* b, double* x,
+                                exg_cg_result* result, void* stream);
+
 const char* exg_status_string(exg_status status);
 const char* exg_last_error(void);
 

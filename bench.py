@@ -241,6 +241,106 @@ def run_gpu(args):
     return 0
 
 
+SWEEP_CELLS = {1: 128, 2: 85, 3: 64, 4: 51, 5: 43, 6: 37, 7: 32, 8: 26}
+
+
+def run_sweep(args):
+    """Autotuned degree sweep: ~16M DoF per degree, 4 right-hand sides per launch."""
+    import numpy as np
+    import torch
+
+    import exadg_gb300 as E
+    from exadg_gb300 import build as B
+
+    B.build()
+    E.load_library()
+    pk = peaks()
+    rows = []
+    for k in range(1, 9):
+        n = SWEEP_CELLS[k]
+        mesh = E.Mesh(n)
+        for pname, prec in (("f64", E.PREC_F64), ("f64e", E.PREC_F64E), ("f32", E.PREC_F32)):
+            op = E.LaplaceOperator(mesh, k, 1.0, prec)
+            best, timings = op.tune(n_rhs=4)
+            X = op.initialize_dof_vector(4)
+            X.copy_(torch.tensor(np.stack([splitmix_uniform(op.n_dofs, s) for s in (1, 2, 3, 4)]), dtype=X.dtype))
+            Y = torch.empty_like(X)
+            for _ in range(3):
+                op.vmult(Y, X, n_rhs=4)
+            torch.cuda.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            reps = 10
+            e0.record()
+            for _ in range(reps):
+                op.vmult(Y, X, n_rhs=4)
+            e1.record()
+            e1.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            esize = 4 if prec == E.PREC_F32 else 8
+            dofs = 4 * op.n_dofs
+            gbs = 2.0 * esize * dofs / (ms * 1e-3) / 1e9
+            rows.append({"degree": k, "n_cells_1d": n, "precision": pname, "n_dofs_per_rhs": op.n_dofs, "n_rhs": 4,
+                         "ms_per_launch": ms, "dofs_per_s": dofs / (ms * 1e-3), "gb_per_s": gbs,
+                         "hbm_frac": gbs / pk.get("hbm_gbs", 6800.0), "cells_per_block": best,
+                         "tuning_ms": {str(c): t for c, t in timings}})
+            del op, X, Y
+            torch.cuda.synchronize()
+    line = {"metric": "DoF/s of op apply per degree (4 RHS per launch, autotuned)", "unit": "DoF/s",
+            "higher_is_better": True, "mode": "sweep", "data": "synthetic", "rows": rows,
+            "roofline_peak_gbs": pk.get("hbm_gbs")}
+    print(json.dumps(line))
+    return 0
+
+
+def run_solve(args):
+    """Time to a 1e-10 relative residual: plain FP64 CG + FP64 multigrid against CG with the
+    FP32 graph-captured V-cycle (outer operator in FP32-pair arithmetic where available)."""
+    import math
+
+    import torch
+
+    import exadg_gb300 as E
+    from exadg_gb300 import build as B
+    from exadg_gb300 import driver as D
+
+    B.build()
+    E.load_library()
+    out = {}
+    # configuration 2b: Cartesian 64^3, k = 4
+    n, k = args.n_cells, args.degree
+    x64, r64 = D.solve_unit_cube_sine(n, k, E.PREC_F64, E.PREC_F64)
+    xm, rm = D.solve_unit_cube_sine(n, k, E.PREC_F64E, E.PREC_F32)
+    out["cartesian"] = {"n_cells_1d": n, "degree": k, "n_dofs": r64["n_dofs"], "levels": r64["levels"],
+                        "plain_fp64": {kk: r64[kk] for kk in ("iterations", "wall_seconds", "setup_seconds", "rn", "r0")},
+                        "mixed": {kk: rm[kk] for kk in ("iterations", "wall_seconds", "setup_seconds", "rn", "r0")},
+                        "speedup": r64["wall_seconds"] / rm["wall_seconds"],
+                        "solution_rel_diff": float(torch.linalg.norm(xm - x64) / torch.linalg.norm(x64))}
+    del x64, xm
+    # configuration 3: curved 48^3, k = 5, mapping degree = k
+    if not args.skip_curved:
+        nc, kc = 48, 5
+        x64, r64 = D.solve_unit_cube_sine(nc, kc, E.PREC_F64, E.PREC_F64, curved=True)
+        xm, rm = D.solve_unit_cube_sine(nc, kc, E.PREC_F64, E.PREC_F32, curved=True)
+        m = E.Mesh(**D.deformed_unit_cube(nc, degree=kc))
+        o64 = E.LaplaceOperator(m, kc, 1.0, E.PREC_F64)
+        o32 = E.LaplaceOperator(m, kc, 1.0, E.PREC_F32)
+        v = torch.tensor(splitmix_uniform(o64.n_dofs, 1), device="cuda")
+        y64 = o64.vmult(o64.initialize_dof_vector(), v)
+        y32 = o32.vmult(o32.initialize_dof_vector(), v.float())
+        apply_err = float(torch.linalg.norm(y32.double() - y64) / torch.linalg.norm(y64))
+        out["curved"] = {"n_cells_1d": nc, "degree": kc, "n_dofs": r64["n_dofs"], "levels": r64["levels"],
+                         "plain_fp64": {kk: r64[kk] for kk in ("iterations", "wall_seconds", "setup_seconds", "rn", "r0")},
+                         "mixed": {kk: rm[kk] for kk in ("iterations", "wall_seconds", "setup_seconds", "rn", "r0")},
+                         "speedup": r64["wall_seconds"] / rm["wall_seconds"],
+                         "fp32_apply_rel_err_vs_fp64": apply_err,
+                         "solution_rel_diff": float(torch.linalg.norm(xm - x64) / torch.linalg.norm(x64))}
+    line = {"metric": "time to 1e-10 relative residual, mixed (FP32 graph V-cycle) vs plain FP64 CG+MG",
+            "value": out["cartesian"]["mixed"]["wall_seconds"], "unit": "s", "higher_is_better": False,
+            "mode": "solve", "data": "synthetic (manufactured sine solution)", "configs": out}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -251,7 +351,13 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-cells", type=int, default=N_CELLS, help="cells per direction (profiling runs use smaller meshes)")
     ap.add_argument("--degree", type=int, default=DEGREE)
+    ap.add_argument("--mode", default="apply", choices=["apply", "solve", "sweep"])
+    ap.add_argument("--skip-curved", action="store_true")
     args = ap.parse_args()
+    if args.mode == "sweep":
+        return run_sweep(args)
+    if args.mode == "solve":
+        return run_solve(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

@@ -109,7 +109,7 @@ class CGResult(ctypes.Structure):
 # every symbol declared in include/exadg_gb300.h
 EXPORTED_SYMBOLS = [
     "exg_mesh_create", "exg_mesh_destroy", "exg_sipg_create", "exg_sipg_destroy", "exg_sipg_n_dofs",
-    "exg_sipg_info", "exg_sipg_apply_f64", "exg_sipg_apply_f32", "exg_sipg_inverse_diagonal_f64",
+    "exg_sipg_info", "exg_sipg_tune", "exg_sipg_set_launch_config", "exg_sipg_apply_f64", "exg_sipg_apply_f32", "exg_sipg_inverse_diagonal_f64",
     "exg_sipg_inverse_diagonal_f32", "exg_sipg_quadrature_points", "exg_sipg_rhs", "exg_mg_default_desc",
     "exg_mg_create", "exg_mg_destroy", "exg_mg_vmult", "exg_mg_info_get", "exg_cg_default_desc", "exg_cg_solve",
     "exg_cg_solve_noalloc", "exg_status_string", "exg_last_error",
@@ -138,6 +138,8 @@ def load_library(path=LIB_PATH):
         "exg_sipg_destroy": [P],
         "exg_sipg_n_dofs": [P, ctypes.POINTER(LL)],
         "exg_sipg_info": [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)],
+        "exg_sipg_tune": [P, I, ctypes.POINTER(I), ctypes.POINTER(ctypes.c_float), ctypes.POINTER(I), P],
+        "exg_sipg_set_launch_config": [P, I],
         "exg_sipg_apply_f64": [P, P, P, I, P],
         "exg_sipg_apply_f32": [P, P, P, I, P],
         "exg_sipg_inverse_diagonal_f64": [P, P, P],
@@ -266,6 +268,17 @@ class LaplaceOperator:
         f = _lib.exg_sipg_inverse_diagonal_f32 if self.precision == PREC_F32 else _lib.exg_sipg_inverse_diagonal_f64
         _check(f(self.h, _ptr(diag), _stream(stream)))
         return diag
+
+    def tune(self, n_rhs=1, stream=None):
+        """Autotune the launch variant (cells per block) for this degree / precision / n_rhs."""
+        best = ctypes.c_int()
+        buf = (ctypes.c_float * 16)()
+        cnt = ctypes.c_int(8)
+        _check(_lib.exg_sipg_tune(self.h, n_rhs, ctypes.byref(best), buf, ctypes.byref(cnt), _stream(stream)))
+        return best.value, [(int(buf[2 * i]), float(buf[2 * i + 1])) for i in range(min(cnt.value, 8))]
+
+    def set_launch_config(self, cpb):
+        _check(_lib.exg_sipg_set_launch_config(self.h, cpb))
 
     def quadrature_points(self, stream=None):
         """Cell points [n_cells, (k+1)^3, 3] and face points [n_cells, 6, (k+1)^2, 3] (FP64)."""

@@ -1,5 +1,6 @@
 // C ABI of the library (include/exadg_gb300.h).  Every entry point catches all exceptions and
 // returns a status; the message of the last failure is kept per host thread.
+#include <algorithm>
 #include <cstring>
 #include <string>
 
@@ -104,6 +105,35 @@ exg_status exg_sipg_apply_f32(exg_op* op, const float* src, float* dst, int n_rh
   EXG_CHECK(op->precision == EXG_PREC_F32, EXG_ERR_INVALID, "operator precision is FP64: use exg_sipg_apply_f64");
   EXG_CHECK(src != dst, EXG_ERR_INVALID, "src and dst must not alias");
   op->apply(src, dst, n_rhs, (cudaStream_t)stream);
+  EXG_API_END
+}
+
+exg_status exg_sipg_tune(exg_op* op, int n_rhs, int* launch_config, float* timings_ms, int* n_timings,
+                         void* stream) {
+  EXG_API_BEGIN
+  EXG_CHECK(op, EXG_ERR_INVALID, "null argument");
+  EXG_CHECK(n_rhs >= 1 && n_rhs <= 65535, EXG_ERR_INVALID, "n_rhs out of range");
+  std::vector<std::pair<int, float>> t;
+  int best = op->tune(n_rhs, (cudaStream_t)stream, &t);
+  if (launch_config) *launch_config = best;
+  if (n_timings) {
+    int cap = *n_timings;
+    *n_timings = (int)t.size();
+    for (int i = 0; i < (int)t.size() && i < cap && timings_ms; ++i) {
+      timings_ms[2 * i] = (float)t[i].first;
+      timings_ms[2 * i + 1] = t[i].second;
+    }
+  }
+  EXG_API_END
+}
+
+exg_status exg_sipg_set_launch_config(exg_op* op, int launch_config) {
+  EXG_API_BEGIN
+  EXG_CHECK(op, EXG_ERR_INVALID, "null argument");
+  std::vector<int> o = cart_cpb_options(op->n, op->precision);
+  EXG_CHECK(launch_config == 0 || std::find(o.begin(), o.end(), launch_config) != o.end(), EXG_ERR_INVALID,
+            "launch_config is not one of the tuned cells-per-block values");
+  op->cpb = launch_config;
   EXG_API_END
 }
 

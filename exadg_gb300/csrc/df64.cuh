@@ -120,7 +120,7 @@ __device__ __forceinline__ void store_as<double, df64>(double* p, df64 v) { *p =
 // bytes of the per-cell face header (neighbour index, penalty, kind) in shared memory, rounded to 16
 template <class C>
 __host__ __device__ constexpr size_t smem_head_bytes(int cpb) {
-  return ((size_t)cpb * 6 * (sizeof(long long) + sizeof(C) + sizeof(int)) + 15) / 16 * 16;
+  return ((size_t)cpb * 6 * (sizeof(C) + 2 * sizeof(int)) + 15) / 16 * 16;
 }
 
 }  // namespace exg

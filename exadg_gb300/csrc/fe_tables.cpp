@@ -147,6 +147,18 @@ void build_cart_host(const MeshInfo& m, const FE1D& fe, double ip, CartHost& out
   }
   for (int e = 0; e < 3; ++e) out.pen.inv_h[e] = 1.0 / m.h[e];
   out.pen.factor = ip * (fe.k + 1.0) * (fe.k + 1.0);
+  // IP::calculate_penalty_parameter on a box cell: tau_c = surface / volume with weight 1 on
+  // non-periodic boundary faces and 0.5 elsewhere = sum_e (w_low + w_high) / h_e.  The class of a
+  // cell encodes per direction bit 0 = at the low boundary, bit 1 = at the high boundary.
+  for (int cls = 0; cls < 64; ++cls) {
+    double t = 0;
+    for (int e = 0; e < 3; ++e) {
+      int code = (cls >> (2 * e)) & 3;
+      double wl = (code & 1) ? 1.0 : 0.5, wr = (code & 2) ? 1.0 : 0.5;
+      t += (wl + wr) / m.h[e];
+    }
+    for (int d = 0; d < 3; ++d) out.tauA[d][cls] = out.A[d] * t * out.pen.factor;
+  }
   for (int e = 0; e < 3; ++e) {
     out.mesh.N[e] = m.N[e];
     out.mesh.periodic[e] = m.d.periodic[e];

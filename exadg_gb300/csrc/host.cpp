@@ -82,6 +82,49 @@ void exg_op::diagonal(void* d, bool invert, cudaStream_t s) const {
     general_diagonal(*geo, fe, d, invert, s);
 }
 
+// Autotuner: time every cells-per-block variant of the affine kernel on this operator's mesh,
+// degree and precision (CUDA events, median of 5 launches after 2 warm-up launches) and keep the
+// fastest.  Curved meshes have a single variant.
+int exg_op::tune(int n_rhs, cudaStream_t s, std::vector<std::pair<int, float>>* timings) {
+  if (!cartesian) return 0;
+  std::vector<int> opts = cart_cpb_options(n, precision);
+  size_t bytes = (size_t)n_dofs() * n_rhs * (precision == EXG_PREC_F32 ? 4 : 8);
+  void* x = dalloc(bytes);
+  void* y = dalloc(bytes);
+  vec_fill(x, precision, 1.0, n_dofs() * n_rhs, s);
+  cudaEvent_t e0, e1;
+  EXG_CUDA(cudaEventCreate(&e0));
+  EXG_CUDA(cudaEventCreate(&e1));
+  int best = opts.empty() ? 0 : opts[0];
+  float best_ms = 1e30f;
+  for (int c : opts) {
+    cpb = c;
+    for (int w = 0; w < 2; ++w) apply(x, y, n_rhs, s);
+    std::vector<float> t;
+    for (int r = 0; r < 5; ++r) {
+      EXG_CUDA(cudaEventRecord(e0, s));
+      apply(x, y, n_rhs, s);
+      EXG_CUDA(cudaEventRecord(e1, s));
+      EXG_CUDA(cudaEventSynchronize(e1));
+      float ms;
+      EXG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+      t.push_back(ms);
+    }
+    std::sort(t.begin(), t.end());
+    if (timings) timings->push_back({c, t[2]});
+    if (t[2] < best_ms) {
+      best_ms = t[2];
+      best = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(x);
+  cudaFree(y);
+  cpb = best;
+  return best;
+}
+
 void exg_op::ensure_rhs_geometry(cudaStream_t s) {
   if (rhs_geo) return;
   rhs_geo.reset(new GeneralGeom());

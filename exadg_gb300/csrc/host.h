@@ -37,6 +37,7 @@ struct exg_op {
   void quadrature_points(double* cx, double* fx, long long* ncp, long long* nfp, cudaStream_t s);
   void rhs(const double* f, const double* g, const double* h, double* b, cudaStream_t s);
   void ensure_rhs_geometry(cudaStream_t s);
+  int tune(int n_rhs, cudaStream_t s, std::vector<std::pair<int, float>>* timings);
 };
 
 namespace exg {

@@ -84,6 +84,7 @@ struct CartHost {
   double sdL[3][9], sdR[3][9];
   double A[3];
   CartPenalty pen;
+  double tauA[3][64];  // A_d * tau_c * (k+1)^2 IP per boundary class of the cell (see cell_class)
   CartMesh mesh;
 };
 void build_cart_host(const MeshInfo& m, const FE1D& fe, double ip, CartHost& out);

@@ -30,9 +30,7 @@ struct CartCoef {
   C M[N * N];
   C B[3][N * N];
   C sdL[3][N], sdR[3][N];
-  double A[3];
-  double inv_h[3];
-  double factor;
+  C tauA[3][64];  // A_d * tau_c * (k+1)^2 IP per cell boundary class
 };
 
 template <int N, class C>
@@ -45,67 +43,81 @@ static CartCoef<N, C> make_coef(const CartHost& h) {
       c.sdL[d][i] = coef_from_double<C>(h.sdL[d][i]);
       c.sdR[d][i] = coef_from_double<C>(h.sdR[d][i]);
     }
-    c.A[d] = h.A[d];
-    c.inv_h[d] = h.pen.inv_h[d];
+    for (int cls = 0; cls < 64; ++cls) c.tauA[d][cls] = coef_from_double<C>(h.tauA[d][cls]);
   }
-  c.factor = h.pen.factor;
   return c;
 }
 
 // --------------------------------------------------------------------------------------------
 // cell / face bookkeeping
 // --------------------------------------------------------------------------------------------
-__device__ __forceinline__ void cell_coords(const CartMesh& m, long long c, int ci[3]) {
-  ci[0] = (int)(c % m.N[0]);
-  long long r = c / m.N[0];
-  ci[1] = (int)(r % m.N[1]);
-  ci[2] = (int)(r / m.N[1]);
+__device__ __forceinline__ void cell_coords(const CartMesh& m, int c, int ci[3]) {
+  const unsigned int uc = (unsigned int)c, n0 = (unsigned int)m.N[0], n1 = (unsigned int)m.N[1];
+  const unsigned int r = uc / n0;
+  ci[0] = (int)(uc - r * n0);
+  ci[1] = (int)(r % n1);
+  ci[2] = (int)(r / n1);
 }
 
-// IP::calculate_penalty_parameter on a box cell: surface/volume with weight 1 on non-periodic
-// boundary faces and 0.5 elsewhere (interior_penalty_parameter.h:45-97)
-__device__ __forceinline__ double cell_tau(const CartMesh& m, const double inv_h[3], const int ci[3]) {
-  double t = 0.0;
+// boundary class of a cell (2 bits per direction: at the low / at the high non-periodic boundary);
+// the penalty tau_c = surface/volume of IP::calculate_penalty_parameter
+// (interior_penalty_parameter.h:45-97) depends on nothing else on a uniform box mesh
+__device__ __forceinline__ int cell_class(const CartMesh& m, const int ci[3]) {
+  int cls = 0;
+#pragma unroll
   for (int e = 0; e < 3; ++e) {
-    double wl = (ci[e] == 0 && !m.periodic[e]) ? 1.0 : 0.5;
-    double wr = (ci[e] == m.N[e] - 1 && !m.periodic[e]) ? 1.0 : 0.5;
-    t += (wl + wr) * inv_h[e];
+    int lo = (ci[e] == 0 && !m.periodic[e]) ? 1 : 0;
+    int hi = (ci[e] == m.N[e] - 1 && !m.periodic[e]) ? 2 : 0;
+    cls |= (lo | hi) << (2 * e);
   }
-  return t;
+  return cls;
 }
+
+__device__ __forceinline__ double cmax(double a, double b) { return fmax(a, b); }
+__device__ __forceinline__ float cmax(float a, float b) { return fmaxf(a, b); }
+__device__ __forceinline__ df64 cmax(df64 a, df64 b) {
+  return (a.hi > b.hi || (a.hi == b.hi && a.lo >= b.lo)) ? a : b;
+}
+__device__ __forceinline__ double ctwice(double a) { return 2.0 * a; }
+__device__ __forceinline__ float ctwice(float a) { return 2.0f * a; }
+__device__ __forceinline__ df64 ctwice(df64 a) { return df64(2.0f * a.hi, 2.0f * a.lo); }
 
 // face f = 2d + side of cell c: neighbour index (or -1), kind (0 interior/periodic, 1 Dirichlet,
-// 2 Neumann) and A_d * tau' (tau' = tau_face interior, 2 tau_c Dirichlet, 0 Neumann)
+// 2 Neumann) and A_d * tau' (tau' = max(tau-, tau+) interior, 2 tau_c Dirichlet, 0 Neumann)
 template <int N, class C>
-__device__ __forceinline__ void face_info(const CartMesh& m, const CartCoef<N, C>& P, long long c, int f,
-                                          long long& nb, int& kind, double& atau) {
+__device__ __forceinline__ void face_info(const CartMesh& m, const CartCoef<N, C>& P, int c, int f, int& nb,
+                                          int& kind, C& atau) {
   int ci[3];
   cell_coords(m, c, ci);
-  int d = f >> 1, side = f & 1;
-  long long stride = d == 0 ? 1 : (d == 1 ? (long long)m.N[0] : (long long)m.N[0] * m.N[1]);
-  int cd = ci[d];
-  double tc = cell_tau(m, P.inv_h, ci) * P.factor;
+  const int d = f >> 1, side = f & 1;
+  const int stride = d == 0 ? 1 : (d == 1 ? m.N[0] : m.N[0] * m.N[1]);
+  const int cd = ci[d];
+  const C tc = P.tauA[d][cell_class(m, ci)];
   nb = -1;
+  int cn[3] = {ci[0], ci[1], ci[2]};
   if (side == 1) {
-    if (cd + 1 < m.N[d])
+    if (cd + 1 < m.N[d]) {
       nb = c + stride;
-    else if (m.periodic[d])
-      nb = c - (long long)(m.N[d] - 1) * stride;
+      cn[d] = cd + 1;
+    } else if (m.periodic[d]) {
+      nb = c - (m.N[d] - 1) * stride;
+      cn[d] = 0;
+    }
   } else {
-    if (cd > 0)
+    if (cd > 0) {
       nb = c - stride;
-    else if (m.periodic[d])
-      nb = c + (long long)(m.N[d] - 1) * stride;
+      cn[d] = cd - 1;
+    } else if (m.periodic[d]) {
+      nb = c + (m.N[d] - 1) * stride;
+      cn[d] = m.N[d] - 1;
+    }
   }
   if (nb >= 0) {
-    int cn[3];
-    cell_coords(m, nb, cn);
-    double tn = cell_tau(m, P.inv_h, cn) * P.factor;
     kind = 0;
-    atau = P.A[d] * fmax(tc, tn);
+    atau = cmax(tc, P.tauA[d][cell_class(m, cn)]);
   } else {
     kind = m.bc[f] == EXG_BC_DIRICHLET ? 1 : 2;
-    atau = kind == 1 ? 2.0 * P.A[d] * tc : 0.0;
+    atau = kind == 1 ? ctwice(tc) : C(0);
   }
 }
 
@@ -118,7 +130,7 @@ __device__ __forceinline__ int line_index(int i, int a, int b) {
 template <int D, int N, class T, class C>
 __device__ __forceinline__ void line_operator(const C* __restrict__ su, C* __restrict__ wout, int a, int b,
                                               const CartCoef<N, C>& P, const T* __restrict__ src,
-                                              const long long* nb, const int* kind, const C* atau) {
+                                              const int* nb, const int* kind, const C* atau) {
   constexpr int N3 = N * N * N;
   C u[N], w[N];
 #pragma unroll
@@ -135,7 +147,7 @@ __device__ __forceinline__ void line_operator(const C* __restrict__ su, C* __res
   w[N - 1] = fmadd(tR, u[N - 1], w[N - 1]);
   // left face
   if (kind[2 * D] == 0) {
-    const T* ln = src + nb[2 * D] * N3;
+    const T* ln = src + (long long)nb[2 * D] * N3;
     C un[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) un[i] = load_as<C>(ln + line_index<D, N>(i, a, b));
@@ -159,7 +171,7 @@ __device__ __forceinline__ void line_operator(const C* __restrict__ su, C* __res
   }
   // right face
   if (kind[2 * D + 1] == 0) {
-    const T* rn = src + nb[2 * D + 1] * N3;
+    const T* rn = src + (long long)nb[2 * D + 1] * N3;
     C un[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) un[i] = load_as<C>(rn + line_index<D, N>(i, a, b));
@@ -205,9 +217,9 @@ __global__ void __launch_bounds__(CPB* N* N) cart_apply_kernel(const T* __restri
                                                                const CartMesh m) {
   constexpr int N2 = N * N, N3 = N2 * N, NT = CPB * N2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  long long* snb = reinterpret_cast<long long*>(smem_raw);  // CPB*6
-  C* stau = reinterpret_cast<C*>(snb + CPB * 6);            // CPB*6
-  int* skind = reinterpret_cast<int*>(stau + CPB * 6);      // CPB*6
+  C* stau = reinterpret_cast<C*>(smem_raw);             // CPB*6
+  int* snb = reinterpret_cast<int*>(stau + CPB * 6);     // CPB*6
+  int* skind = snb + CPB * 6;                            // CPB*6
   C* su = reinterpret_cast<C*>(smem_raw + smem_head_bytes<C>(CPB));
   C* wx = su + CPB * N3;
   C* wy = wx + CPB * N3;
@@ -225,13 +237,12 @@ __global__ void __launch_bounds__(CPB* N* N) cart_apply_kernel(const T* __restri
   for (int t = tid; t < CPB * 6; t += NT) {  // NT < 6 CPB for k = 1
     int lc = t / 6, f = t - lc * 6;
     long long c = c0 + lc;
-    long long nb = -1;
-    int kind = 2;
-    double at = 0.0;
-    if (c < m.n_cells) face_info<N, C>(m, P, c, f, nb, kind, at);
+    int nb = -1, kind = 2;
+    C at = C(0);
+    if (c < m.n_cells) face_info<N, C>(m, P, (int)c, f, nb, kind, at);
     snb[t] = nb;
     skind[t] = kind;
-    stau[t] = coef_from_double<C>(at);
+    stau[t] = at;
   }
   __syncthreads();
 
@@ -255,24 +266,24 @@ __global__ void __launch_bounds__(CPB* N* N) cart_apply_kernel(const T* __restri
   }
   __syncthreads();
   if (active) {
-    // z-line (i = a, j = b): y = M_z (wx + wy) + wz
+    // z-line (i = a, j = b): y = M_z (wx + wy) + wz, stored straight to global memory (for a
+    // fixed k the threads of a cell write N*N consecutive values)
     C v[N];
 #pragma unroll
     for (int k = 0; k < N; ++k) {
       int id = line_index<2, N>(k, a, b);
       v[k] = wx[co + id] + wy[co + id];
     }
+    T* oc = o + base + co;
 #pragma unroll
     for (int k = 0; k < N; ++k) {
       int id = line_index<2, N>(k, a, b);
       C acc = wz[co + id];
 #pragma unroll
       for (int j = 0; j < N; ++j) acc = fmadd(P.M[k * N + j], v[j], acc);
-      su[co + id] = acc;
+      store_as<T>(oc + id, acc);
     }
   }
-  __syncthreads();
-  for (int i = tid; i < nd; i += NT) store_as<T>(o + base + i, su[i]);
 }
 
 // diagonal: sum_d diag(A_d L_d^self)[i_d] * M[i_e][i_e] * M[i_f][i_f]
@@ -292,20 +303,18 @@ __global__ void cart_diag_kernel(T* __restrict__ diag, const __grid_constant__ C
     int i = idx[d];
     double v = coef_to_double(P.B[d][i * N + i]);
     if (i == 0) {
-      long long nb;
-      int kind;
-      double at;
-      face_info<N, C>(m, P, c, 2 * d, nb, kind, at);
-      v += at;
+      int nb, kind;
+      C at;
+      face_info<N, C>(m, P, (int)c, 2 * d, nb, kind, at);
+      v += coef_to_double(at);
       if (kind == 1) v += 2.0 * coef_to_double(P.sdL[d][0]);
       if (kind == 2) v -= 2.0 * coef_to_double(P.sdL[d][0]);
     }
     if (i == N - 1) {
-      long long nb;
-      int kind;
-      double at;
-      face_info<N, C>(m, P, c, 2 * d + 1, nb, kind, at);
-      v += at;
+      int nb, kind;
+      C at;
+      face_info<N, C>(m, P, (int)c, 2 * d + 1, nb, kind, at);
+      v += coef_to_double(at);
       if (kind == 1) v -= 2.0 * coef_to_double(P.sdR[d][N - 1]);
       if (kind == 2) v += 2.0 * coef_to_double(P.sdR[d][N - 1]);
     }
@@ -322,14 +331,14 @@ __global__ void cart_diag_kernel(T* __restrict__ diag, const __grid_constant__ C
 // --------------------------------------------------------------------------------------------
 template <int N>
 struct CpbChoice;
-template <> struct CpbChoice<2> { static constexpr int a = 32, b = 64; };
-template <> struct CpbChoice<3> { static constexpr int a = 16, b = 32; };
-template <> struct CpbChoice<4> { static constexpr int a = 8, b = 16; };
-template <> struct CpbChoice<5> { static constexpr int a = 8, b = 16; };
-template <> struct CpbChoice<6> { static constexpr int a = 4, b = 8; };
-template <> struct CpbChoice<7> { static constexpr int a = 4, b = 8; };
-template <> struct CpbChoice<8> { static constexpr int a = 2, b = 4; };
-template <> struct CpbChoice<9> { static constexpr int a = 2, b = 4; };
+template <> struct CpbChoice<2> { static constexpr int a = 16, b = 32, c = 64; };
+template <> struct CpbChoice<3> { static constexpr int a = 8, b = 16, c = 32; };
+template <> struct CpbChoice<4> { static constexpr int a = 4, b = 8, c = 16; };
+template <> struct CpbChoice<5> { static constexpr int a = 4, b = 8, c = 16; };
+template <> struct CpbChoice<6> { static constexpr int a = 2, b = 4, c = 8; };
+template <> struct CpbChoice<7> { static constexpr int a = 2, b = 4, c = 8; };
+template <> struct CpbChoice<8> { static constexpr int a = 1, b = 2, c = 4; };
+template <> struct CpbChoice<9> { static constexpr int a = 1, b = 2, c = 4; };
 
 template <int N, int CPB, class T, class C>
 static void launch_apply(const CartHost& h, const void* src, void* dst, int n_rhs, cudaStream_t s) {
@@ -352,10 +361,12 @@ static void launch_apply(const CartHost& h, const void* src, void* dst, int n_rh
 
 template <int N, class T, class C>
 static void apply_n(const CartHost& h, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s) {
-  if (cpb == CpbChoice<N>::b)
-    launch_apply<N, CpbChoice<N>::b, T, C>(h, src, dst, n_rhs, s);
-  else
+  if (cpb == CpbChoice<N>::a)
     launch_apply<N, CpbChoice<N>::a, T, C>(h, src, dst, n_rhs, s);
+  else if (cpb == CpbChoice<N>::c)
+    launch_apply<N, CpbChoice<N>::c, T, C>(h, src, dst, n_rhs, s);
+  else
+    launch_apply<N, CpbChoice<N>::b, T, C>(h, src, dst, n_rhs, s);
 }
 
 template <class T, class C>
@@ -384,16 +395,21 @@ void cart_apply(const CartHost& h, int precision, const void* src, void* dst, in
     throw Error{EXG_ERR_INVALID, "unknown precision"};
 }
 
+template <int N>
+static std::vector<int> cpb_list() {
+  return {CpbChoice<N>::a, CpbChoice<N>::b, CpbChoice<N>::c};
+}
+
 std::vector<int> cart_cpb_options(int n, int) {
   switch (n) {
-    case 2: return {CpbChoice<2>::a, CpbChoice<2>::b};
-    case 3: return {CpbChoice<3>::a, CpbChoice<3>::b};
-    case 4: return {CpbChoice<4>::a, CpbChoice<4>::b};
-    case 5: return {CpbChoice<5>::a, CpbChoice<5>::b};
-    case 6: return {CpbChoice<6>::a, CpbChoice<6>::b};
-    case 7: return {CpbChoice<7>::a, CpbChoice<7>::b};
-    case 8: return {CpbChoice<8>::a, CpbChoice<8>::b};
-    case 9: return {CpbChoice<9>::a, CpbChoice<9>::b};
+    case 2: return cpb_list<2>();
+    case 3: return cpb_list<3>();
+    case 4: return cpb_list<4>();
+    case 5: return cpb_list<5>();
+    case 6: return cpb_list<6>();
+    case 7: return cpb_list<7>();
+    case 8: return cpb_list<8>();
+    case 9: return cpb_list<9>();
   }
   return {};
 }

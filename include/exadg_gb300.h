@@ -77,6 +77,16 @@ exg_status exg_sipg_info(const exg_op* op, int* degree, int* precision, int* car
 exg_status exg_sipg_apply_f64(exg_op* op, const double* src, double* dst, int n_rhs, void* stream);
 exg_status exg_sipg_apply_f32(exg_op* op, const float* src, float* dst, int n_rhs, void* stream);
 
+/* Autotuner: times the launch variants of the apply kernel (cells per thread block; one thread
+ * per line of a cell) for this operator's degree, precision and n_rhs, keeps the fastest and
+ * returns it in *launch_config; timings_ms receives (variant, median ms) pairs, *n_timings their
+ * count (in: capacity).  No reference counterpart (deal.II picks its vectorisation at compile time,
+ * operators/operator_base.h:116-117). */
+exg_status exg_sipg_tune(exg_op* op, int n_rhs, int* launch_config, float* timings_ms, int* n_timings,
+                         void* stream);
+/* select a launch variant explicitly (0 = default) */
+exg_status exg_sipg_set_launch_config(exg_op* op, int launch_config);
+
 /* inverse diagonal, |d| <= 1e-10 -> 1
  * (OperatorBase::calculate_inverse_diagonal, operators/operator_base.cpp:251-262;
  *  utilities/invert_diagonal.h:35-46) */

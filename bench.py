@@ -341,6 +341,68 @@ def run_solve(args):
     return 0
 
 
+def run_learned(args):
+    """Pressure-Poisson sequence of the Taylor-Green vortex (32^3 cells, k_p = 2, periodic, Re 1600):
+    CG (FP64, FP32-pair operator) + FP32 multigrid to ||r|| <= 1e-10 ||b||, seeded by BDF2
+    extrapolation or by extrapolation + learned CNN correction."""
+    import statistics
+
+    import torch
+
+    import exadg_gb300 as E
+    from exadg_gb300 import build as B
+    from exadg_gb300 import learned_guess as LG
+
+    B.build()
+    E.load_library()
+    steps = args.learned_steps
+    t0 = time.perf_counter()
+    rhs, dt = LG.tgv_rhs_sequence(steps, n_cells=32, degree=2)
+    gen_s = time.perf_counter() - t0
+    res = {}
+    for mode in ("extrapolation", "untrained", "learned"):
+        seq = LG.PressureSequence(n_cells=32, degree=2, mode=mode, train_every=20, epochs=args.learned_epochs)
+        seq.diagnostics = args.learned_diagnostics
+        for b in rhs:
+            seq.step(b)
+        log = seq.log
+        tail = [r for r in log if r["step"] >= steps // 2]
+        allw = [r for r in log if r["step"] >= 3]
+        res[mode] = {
+            "mean_iterations_after_step3": statistics.mean(r["iterations"] for r in allw),
+            "mean_iterations_second_half": statistics.mean(r["iterations"] for r in tail),
+            "mean_solve_s_second_half": statistics.mean(r["solve_s"] for r in tail),
+            "mean_guess_s_second_half": statistics.mean(r["guess_s"] for r in tail),
+            "mean_total_s_second_half": statistics.mean(r["solve_s"] + r["guess_s"] for r in tail),
+            "mean_r0_rel_second_half": statistics.mean(r["r0_rel"] for r in tail),
+            "sources": {s_: sum(1 for r in log if r["source"] == s_) for s_ in ("zero", "previous", "extrapolation",
+                                                                              "learned", "fallback")},
+            "mean_r_ext_rel_second_half": statistics.mean(r.get("r_ext_rel", r["r0_rel"]) for r in tail),
+            "train_s_total": sum(r.get("train_s", 0.0) for r in log),
+            "iterations": [r["iterations"] for r in log],
+        }
+        d3 = [r["r_ext3_rel"] for r in tail if "r_ext3_rel" in r]
+        if d3:
+            res[mode]["mean_r_ext3_rel_second_half"] = statistics.mean(d3)
+        last = [r for r in log if "loss_last" in r]
+        if last:
+            res[mode]["loss_first_round"] = last[0]["loss_first"]
+            res[mode]["loss_last_round"] = last[-1]["loss_last"]
+        del seq
+        torch.cuda.synchronize()
+    e, l, u = res["extrapolation"], res["learned"], res["untrained"]
+    line = {"metric": "PPE CG iterations per solve, learned guess vs BDF2 extrapolation (TGV 32^3, k_p=2)",
+            "value": l["mean_iterations_second_half"], "unit": "iterations", "higher_is_better": False,
+            "mode": "learned", "data": "synthetic: TGV Re=1600 pressure sources from a pseudo-spectral integrator",
+            "steps": steps, "dt": dt, "rhs_generation_s": gen_s,
+            "iteration_gain_second_half": e["mean_iterations_second_half"] - l["mean_iterations_second_half"],
+            "iteration_gain_trained_vs_untrained": u["mean_iterations_second_half"] - l["mean_iterations_second_half"],
+            "time_gain_second_half": e["mean_total_s_second_half"] / l["mean_total_s_second_half"],
+            "results": res}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -351,13 +413,18 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-cells", type=int, default=N_CELLS, help="cells per direction (profiling runs use smaller meshes)")
     ap.add_argument("--degree", type=int, default=DEGREE)
-    ap.add_argument("--mode", default="apply", choices=["apply", "solve", "sweep"])
+    ap.add_argument("--mode", default="apply", choices=["apply", "solve", "sweep", "learned"])
+    ap.add_argument("--learned-steps", type=int, default=400)
+    ap.add_argument("--learned-epochs", type=int, default=40)
+    ap.add_argument("--learned-diagnostics", action="store_true")
     ap.add_argument("--skip-curved", action="store_true")
     args = ap.parse_args()
     if args.mode == "sweep":
         return run_sweep(args)
     if args.mode == "solve":
         return run_solve(args)
+    if args.mode == "learned":
+        return run_learned(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

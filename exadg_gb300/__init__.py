@@ -113,6 +113,8 @@ EXPORTED_SYMBOLS = [
     "exg_sipg_inverse_diagonal_f32", "exg_sipg_quadrature_points", "exg_sipg_rhs", "exg_mg_default_desc",
     "exg_mg_create", "exg_mg_destroy", "exg_mg_vmult", "exg_mg_info_get", "exg_cg_default_desc", "exg_cg_solve",
     "exg_cg_solve_noalloc", "exg_status_string", "exg_last_error",
+    "exg_cnn_create", "exg_cnn_destroy", "exg_cnn_n_params", "exg_cnn_params", "exg_cnn_forward",
+    "exg_cnn_backward", "exg_cnn_train_step", "exg_cnn_adam", "exg_dg_pack", "exg_dg_unpack_add", "exg_dg_pack_diff",
 ]
 
 _lib = None
@@ -154,6 +156,17 @@ def load_library(path=LIB_PATH):
         "exg_cg_default_desc": [ctypes.POINTER(CGDesc)],
         "exg_cg_solve": [P, P, ctypes.POINTER(CGDesc), P, P, ctypes.POINTER(CGResult), P],
         "exg_cg_solve_noalloc": [P, ctypes.POINTER(CGDesc), P, P, ctypes.POINTER(CGResult), P],
+        "exg_cnn_create": [ctypes.POINTER(I), I, I, I, ctypes.c_ulonglong, PP],
+        "exg_cnn_destroy": [P],
+        "exg_cnn_n_params": [P, ctypes.POINTER(LL)],
+        "exg_cnn_params": [P, PP, PP],
+        "exg_cnn_forward": [P, P, P, P],
+        "exg_cnn_backward": [P, P, P, P],
+        "exg_cnn_train_step": [P, P, P, ctypes.c_float, ctypes.POINTER(ctypes.c_float), P],
+        "exg_cnn_adam": [P, ctypes.c_float, P],
+        "exg_dg_pack": [P, P, I, I, LL, P, P],
+        "exg_dg_unpack_add": [P, P, D, I, LL, P, P],
+        "exg_dg_pack_diff": [P, P, D, I, LL, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

@@ -26,6 +26,7 @@ SOURCES = [
     "host.cpp",
     "capi.cpp",
     "noalloc.cu",
+    "cnn.cu",
 ]
 
 

@@ -125,6 +125,26 @@ int exg_op::tune(int n_rhs, cudaStream_t s, std::vector<std::pair<int, float>>* 
   return best;
 }
 
+CGWorkspace& exg_op::workspace() {
+  if (!ws) {
+    ws.reset(new CGWorkspace());
+    long long n = n_dofs();
+    ws->r = (double*)dalloc(n * 8);
+    ws->z = (double*)dalloc(n * 8);
+    ws->p = (double*)dalloc(n * 8);
+    ws->v = (double*)dalloc(n * 8);
+    ws->dinv = (double*)dalloc(n * 8);
+    ws->red = Reduction::create();
+  }
+  return *ws;
+}
+
+CGWorkspace::~CGWorkspace() {
+  for (double* ptr : {r, z, p, v, dinv})
+    if (ptr) cudaFree(ptr);
+  red.destroy();
+}
+
 void exg_op::ensure_rhs_geometry(cudaStream_t s) {
   if (rhs_geo) return;
   rhs_geo.reset(new GeneralGeom());
@@ -538,13 +558,17 @@ void exg_mg::info(exg_mg_info& out) const {
 exg_status exg::cg_solve(exg_op& op, exg_mg* mg, const exg_cg_desc& d, const double* b, double* x, exg_cg_result& res,
                          cudaStream_t s) {
   long long n = op.n_dofs();
-  double *r = (double*)dalloc(n * 8), *z = (double*)dalloc(n * 8), *p = (double*)dalloc(n * 8),
-         *v = (double*)dalloc(n * 8);
+  // work vectors live with the operator and are reused by later solves
+  CGWorkspace& w = op.workspace();
+  double *r = w.r, *z = w.z, *p = w.p, *v = w.v;
+  Reduction& red = w.red;
   double* dinv = nullptr;
-  Reduction red = Reduction::create();
   if (d.precond == 1) {
-    dinv = (double*)dalloc(n * 8);
-    op.diagonal(dinv, true, s);
+    if (!w.dinv_valid) {
+      op.diagonal(w.dinv, true, s);
+      w.dinv_valid = true;
+    }
+    dinv = w.dinv;
   }
   EXG_CUDA(cudaStreamSynchronize(s));
   auto t0 = std::chrono::steady_clock::now();
@@ -561,9 +585,6 @@ exg_status exg::cg_solve(exg_op& op, exg_mg* mg, const exg_cg_desc& d, const dou
   CGStats st = pcg_run<double>(A, P, b, x, n, d.rel_tol, d.abs_tol, d.max_iter, false, false, r, z, p, v, red, s);
   EXG_CUDA(cudaStreamSynchronize(s));
   auto t1 = std::chrono::steady_clock::now();
-  red.destroy();
-  for (double* ptr : {r, z, p, v, dinv})
-    if (ptr) cudaFree(ptr);
   res.iterations = st.its;
   res.converged = st.status == 0;
   res.r0 = st.r0;

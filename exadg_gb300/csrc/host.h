@@ -17,6 +17,16 @@ namespace exg {
 MeshInfo make_mesh_info(const exg_mesh_desc& d);
 }
 
+namespace exg {
+// CG work vectors kept with an operator between solves
+struct CGWorkspace {
+  double *r = nullptr, *z = nullptr, *p = nullptr, *v = nullptr, *dinv = nullptr;
+  bool dinv_valid = false;
+  Reduction red;
+  ~CGWorkspace();
+};
+}  // namespace exg
+
 // SIPG Laplace operator (Poisson::LaplaceOperator)
 struct exg_op {
   exg::MeshInfo mesh;
@@ -38,6 +48,8 @@ struct exg_op {
   void rhs(const double* f, const double* g, const double* h, double* b, cudaStream_t s);
   void ensure_rhs_geometry(cudaStream_t s);
   int tune(int n_rhs, cudaStream_t s, std::vector<std::pair<int, float>>* timings);
+  exg::CGWorkspace& workspace();
+  std::unique_ptr<exg::CGWorkspace> ws;
 };
 
 namespace exg {

@@ -1,0 +1,226 @@
+"""Learned initial guess for the sequence of pressure-Poisson solves (row a20).
+
+ExaDG seeds every pressure solve of the dual-splitting scheme with the polynomial extrapolation
+p0 = sum_i beta_i p^{n-i}, beta = (2, -1) for BDF2 (time_int_bdf_dual_splitting.cpp:489-498,
+time_integration/extrapolation_constants.cpp:55-80).  Here a cell-patch CNN (csrc/cnn.cu) predicts a
+correction to that extrapolation from, per cell, the DG coefficients of the last three pressures
+(p^n and its first and second backward differences) and of the current right-hand side (entering as
+the residual of the extrapolation, b - A p_ext).  It is trained online on the solver's own
+converged pressures every `train_every` steps in the energy norm that CG minimises,
+L = (d - e)^T A (d - e) / d^T A d with d = p - p_ext and e = s y(x) (A (d - e) = r_ext - A e, so the
+gradient costs one operator apply).  At inference the correction is scaled by the one-term
+least-squares coefficient c = <r_ext, A e> / ||A e||^2, so the learned guess p_ext + c e never has a
+larger residual than p_ext; whenever it does not have a strictly smaller initial residual the plain
+extrapolation is used (fallback).  Both seedings run FP64 CG + FP32 multigrid to the same
+tolerance, ||r|| <= tol * ||b||.
+"""
+import ctypes
+import time
+
+import exadg_gb300 as E
+from exadg_gb300.cnn import CellPatchCNN
+
+
+def _rms(t):
+    import torch
+
+    return float(torch.linalg.norm(t)) / (t.numel() ** 0.5)
+
+
+class PressureSequence:
+    def __init__(self, n_cells=32, degree=2, length=6.283185307179586, mode="learned", train_every=20,
+                 epochs=40, lr=1e-3, buffer=20, hidden=32, seed=1, tol=1e-10, outer_precision=E.PREC_F64E):
+        import torch
+
+        self.torch = torch
+        kw = dict(n_cells=(n_cells,) * 3, hi=(length,) * 3, periodic=(1, 1, 1))
+        self.mesh = E.Mesh(**kw)
+        self.op = E.LaplaceOperator(self.mesh, degree, 1.0, outer_precision)
+        self.op.tune()
+        self.mg = E.MultigridPreconditioner(self.op, mg_precision=E.PREC_F32, singular=True)
+        self.n_cells = n_cells
+        self.nc = n_cells ** 3
+        self.dpc = (degree + 1) ** 3
+        self.mode = mode
+        self.train_every = train_every
+        self.epochs = epochs
+        self.lr = lr
+        self.buffer_size = buffer
+        self.tol = tol
+        self.hist = []  # converged pressures, newest last
+        self.samples = []
+        self.cnn = None
+        if mode in ("learned", "untrained"):
+            self.cnn = CellPatchCNN((n_cells,) * 3, 4 * self.dpc, hidden, self.dpc, seed)
+            # the linear skip starts as the third-order extrapolation term: output = input channels of
+            # the second backward difference p^n - 2 p^{n-1} + p^{n-2}
+            off = sum(int(torch.tensor(sh).prod()) for _, sh in self.cnn.layer_shapes()[:6])
+            w4 = self.cnn.params[off:off + self.dpc * 4 * self.dpc].view(self.dpc, 4 * self.dpc)
+            w4.zero_()
+            w4[:, 2 * self.dpc:3 * self.dpc] += torch.eye(self.dpc, device="cuda")
+        self.trained = mode == "untrained"
+        self.delta_scale = None
+        self.x = torch.empty((4 * self.dpc, self.nc), dtype=torch.float32, device="cuda")
+        self.log = []
+        n = self.op.n_dofs
+        self.tmp = torch.empty(n, dtype=torch.float64, device="cuda")
+        self.ptrs = torch.empty(4, dtype=torch.int64, device="cuda")
+        self.inv_scales = torch.empty(4, dtype=torch.float64, device="cuda")
+        self.diagnostics = False
+
+    # ------------------------------------------------------------------------------------------
+    def _residual(self, b, x):
+        self.op.vmult(self.tmp, x)
+        return b - self.tmp
+
+    def _features(self, b, p_ext):
+        torch = self.torch
+        p0, p1, p2 = self.hist[-1], self.hist[-2], self.hist[-3]
+        d1 = p0 - p1
+        d2 = p0 - 2 * p1 + p2
+        r = self._residual(b, p_ext)
+        vecs = [p0, d1, d2, r]
+        sc = [max(_rms(v), 1e-300) for v in vecs]
+        self.ptrs.copy_(torch.tensor([v.data_ptr() for v in vecs], dtype=torch.int64))
+        self.inv_scales.copy_(torch.tensor([1.0 / s for s in sc], dtype=torch.float64))
+        E._check(E._lib.exg_dg_pack(ctypes.c_void_p(self.ptrs.data_ptr()), ctypes.c_void_p(self.inv_scales.data_ptr()),
+                                    4, self.dpc, self.nc, E._ptr(self.x), E._stream()))
+        return vecs  # keep tensors alive until the pack has run
+
+    def initial_guess(self, b):
+        """Returns (guess, info)."""
+        torch = self.torch
+        info = {"source": "zero"}
+        if len(self.hist) == 0:
+            return torch.zeros_like(b), info
+        if len(self.hist) == 1:
+            info["source"] = "previous"
+            return self.hist[-1].clone(), info
+        p_ext = 2 * self.hist[-1] - self.hist[-2]
+        info["source"] = "extrapolation"
+        if self.cnn is None or len(self.hist) < 3 or not self.trained or self.delta_scale is None:
+            return p_ext, info
+        keep = self._features(b, p_ext)
+        r_ext = keep[3]
+        y = self.cnn.forward(self.x)
+        e = torch.empty_like(p_ext)
+        E._check(E._lib.exg_dg_unpack_add(E._ptr(y), E._ptr(torch.zeros_like(p_ext)), self.delta_scale, self.dpc,
+                                          self.nc, E._ptr(e), E._stream()))
+        Ae = torch.empty_like(p_ext)
+        self.op.vmult(Ae, e)
+        aa = float(Ae @ Ae)
+        c = float(r_ext @ Ae) / aa if aa > 0 else 0.0
+        r_ext_n = float(torch.linalg.norm(r_ext))
+        r_cnn_n = float(torch.linalg.norm(r_ext - c * Ae))
+        info.update(r_ext=r_ext_n, r_cnn=r_cnn_n, c=c)
+        if self.diagnostics:  # residual of the third-order extrapolation p_ext + (p^n - 2p^{n-1} + p^{n-2})
+            info["r_ext3"] = float(torch.linalg.norm(self._residual(b, p_ext + keep[2])))
+        del keep
+        if c > 0 and r_cnn_n < r_ext_n:
+            info["source"] = "learned"
+            return p_ext + c * e, info
+        info["source"] = "fallback"
+        return p_ext, info
+
+    def _record_sample(self, b, p_new):
+        """Training sample: features at the state before the solve and r_ext = b - A p_ext."""
+        if self.cnn is None or len(self.hist) < 3:
+            return
+        p_ext = 2 * self.hist[-1] - self.hist[-2]
+        keep = self._features(b, p_ext)
+        delta = p_new - p_ext
+        s = _rms(delta)
+        self.delta_scale = s if self.delta_scale is None else 0.8 * self.delta_scale + 0.2 * s
+        r_ext = keep[3].clone()
+        del keep
+        self.samples.append((self.x.clone(), r_ext, delta))
+        if len(self.samples) > self.buffer_size:
+            self.samples.pop(0)
+
+    def _train(self):
+        """Adam steps on L = (d - e)^T A (d - e) / d^T A d with e = s y(x) in DG layout:
+        dL/de = -2 (r_ext - A e) / (d . r_ext) (A symmetric, A d = r_ext); dL/dy = s dL/de."""
+        torch = self.torch
+        s = self.delta_scale
+        zero = torch.zeros(self.op.n_dofs, dtype=torch.float64, device="cuda")
+        e = torch.empty_like(zero)
+        Ae = torch.empty_like(zero)
+        gy = torch.empty((self.dpc, self.nc), dtype=torch.float32, device="cuda")
+        losses = []
+        for it in range(self.epochs):
+            x, r_ext, d = self.samples[it % len(self.samples)]
+            nrm = float(d @ r_ext)
+            y = self.cnn.forward(x)
+            E._check(E._lib.exg_dg_unpack_add(E._ptr(y), E._ptr(zero), s, self.dpc, self.nc, E._ptr(e), E._stream()))
+            self.op.vmult(Ae, e)
+            res = r_ext - Ae
+            losses.append(float((d - e) @ res) / nrm)
+            # gy[i][c] = s * (-2 / nrm) * res[c*dpc + i]
+            E._check(E._lib.exg_dg_pack_diff(E._ptr(zero), E._ptr(res), 2.0 * s / nrm, self.dpc, self.nc,
+                                             E._ptr(gy), E._stream()))
+            self.cnn.backward(x, gy)
+            self.cnn.adam(self.lr)
+        self.trained = True
+        return losses
+
+    # ------------------------------------------------------------------------------------------
+    def step(self, b):
+        torch = self.torch
+        b = b - b.mean()  # singular periodic problem: project the rhs (operator_projection_methods.cpp)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        x, info = self.initial_guess(b)
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        bn = float(torch.linalg.norm(b))
+        solver = E.KrylovSolver(self.op, self.mg, rel_tol=1e-30, abs_tol=self.tol * bn, max_iter=1000)
+        its = solver.solve(x, b)
+        x -= x.mean()  # fix the pressure level of the singular problem
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        rec = dict(step=len(self.log), iterations=its, solve_s=t2 - t1, guess_s=t1 - t0, source=info["source"],
+                   r0_rel=solver.result["r0"] / bn)
+        if "r_ext" in info:
+            rec["r_ext_rel"] = info["r_ext"] / bn
+            rec["r_cnn_rel"] = info["r_cnn"] / bn
+        if self.mode == "untrained":
+            self.samples.clear()
+        if "r_ext3" in info:
+            rec["r_ext3_rel"] = info["r_ext3"] / bn
+        self._record_sample(b, x)
+        self.hist.append(x)
+        if len(self.hist) > 3:
+            self.hist.pop(0)
+        if self.mode == "learned" and len(self.samples) > 0 and (len(self.log) + 1) % self.train_every == 0:
+            torch.cuda.synchronize()
+            t3 = time.perf_counter()
+            losses = self._train()
+            torch.cuda.synchronize()
+            rec["train_s"] = time.perf_counter() - t3
+            rec["loss_first"] = losses[0]
+            rec["loss_last"] = losses[-1]
+        self.log.append(rec)
+        return x, rec
+
+
+def tgv_rhs_sequence(n_steps, n_cells=32, degree=2, dt=None, modes=64, device="cuda"):
+    """Right-hand sides b^n = (f^n, v) of the DG pressure-Poisson problem along a TGV run."""
+    import math
+
+    import torch
+
+    from exadg_gb300.tgv import TGVSpectral, dg_quadrature_grid, grid_to_cells
+
+    if dt is None:  # CFL 0.3 with the velocity degree 3 on n_cells: dt = 0.3 h / (u_max k_u^1.5)
+        dt = 0.3 * (2 * math.pi / n_cells) / (3 ** 1.5)
+    flow = TGVSpectral(modes=modes, dt=dt, device=device)
+    mesh = E.Mesh((n_cells,) * 3, hi=(2 * math.pi,) * 3, periodic=(1, 1, 1))
+    op = E.LaplaceOperator(mesh, degree, 1.0, E.PREC_F64)
+    xs = dg_quadrature_grid(n_cells, degree + 1, device=device)
+    out = []
+    for _ in range(n_steps):
+        flow.step()
+        F = flow.evaluate(flow.pressure_source_hat(), [xs, xs, xs])
+        f = grid_to_cells(F, n_cells, degree + 1)
+        out.append(op.rhs(f_cell=f))
+    return out, dt

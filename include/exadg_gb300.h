@@ -161,6 +161,41 @@ exg_status exg_cg_default_desc(exg_cg_desc* desc);
 exg_status exg_cg_solve(exg_op* op, exg_mg* mg, const exg_cg_desc* desc, const double* b, double* x,
                         exg_cg_result* result, void* stream);
 
+/* ---------------------------------------------------------------------------------------------
+ * Learned initial guess for the pressure-Poisson sequence (the extrapolation p0 = sum_i beta_i p^{n-i}
+ * of TimeIntBDFDualSplitting::pressure_step, incompressible_navier_stokes/time_integration/
+ * time_int_bdf_dual_splitting.cpp:489-498, plus a learned correction).  A cell-patch CNN on the
+ * periodic cell grid: 1x1x1 c_in->c_hidden, 3x3x3 c_hidden->c_hidden, 3x3x3 c_hidden->c_out
+ * (SiLU between layers) plus a linear 1x1x1 skip c_in->c_out; activations channel-major
+ * [C][n_cells] in FP32.  No counterpart in the
+ * reference (the learned correction is an addition); the fallback to plain extrapolation is the
+ * caller's choice of the guess with the smaller initial residual.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct exg_cnn exg_cnn;
+exg_status exg_cnn_create(const int n_cells[3], int c_in, int c_hidden, int c_out, unsigned long long seed,
+                          exg_cnn** cnn);
+exg_status exg_cnn_destroy(exg_cnn* cnn);
+exg_status exg_cnn_n_params(const exg_cnn* cnn, long long* n_params);
+/* device pointers to the parameter vector (W1, b1, W2, b2, W3, b3, W4) and to its gradient */
+exg_status exg_cnn_params(exg_cnn* cnn, float** params, float** grads);
+exg_status exg_cnn_forward(exg_cnn* cnn, const float* x, float* y, void* stream);
+/* gradient of <gy, y(x)> with respect to the parameters, written to the gradient vector */
+exg_status exg_cnn_backward(exg_cnn* cnn, const float* x, const float* gy, void* stream);
+/* one Adam step on the mean-squared error between y(x) and target; *loss = MSE before the step */
+exg_status exg_cnn_train_step(exg_cnn* cnn, const float* x, const float* target, float lr, float* loss,
+                              void* stream);
+/* one Adam step with the gradient currently held by the network (from exg_cnn_backward) */
+exg_status exg_cnn_adam(exg_cnn* cnn, float lr, void* stream);
+/* x[j*dpc + i][c] = vecs[j][c*dpc + i] * inv_scales[j] (vecs, inv_scales: device arrays) */
+exg_status exg_dg_pack(const double* const* vecs, const double* inv_scales, int n_vec, int dofs_per_cell,
+                       long long n_cells, float* x, void* stream);
+/* dst[c*dpc + i] = base[c*dpc + i] + scale * y[i][c] */
+exg_status exg_dg_unpack_add(const float* y, const double* base, double scale, int dofs_per_cell,
+                             long long n_cells, double* dst, void* stream);
+/* t[i][c] = (a[c*dpc + i] - b[c*dpc + i]) * inv_scale */
+exg_status exg_dg_pack_diff(const double* a, const double* b, double inv_scale, int dofs_per_cell,
+                            long long n_cells, float* t, void* stream);
+
 /* The same point-Jacobi / unpreconditioned CG as exg_cg_solve (desc->precond 0 or 1), but it
  * allocates nothing: its work vectors live in one statically allocated device array of about
  * 20 MiB that every GPU loading this library holds until the process exits.  For callers that

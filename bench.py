@@ -156,6 +156,11 @@ def run_gpu(args):
     prec = {"f64": E.PREC_F64, "f32": E.PREC_F32, "f64e": E.PREC_F64E}[args.precision]
     mesh = E.Mesh(args.n_cells)
     op = E.LaplaceOperator(mesh, args.degree, 1.0, prec)
+    if args.launch_config is not None:
+        op.set_launch_config(args.launch_config)
+        launch_config, tuning = args.launch_config, []
+    else:
+        launch_config, tuning = op.tune() if not args.no_tune else (0, [])
     n = op.n_dofs
     dt = op.dtype
     esize = 4 if prec == E.PREC_F32 else 8
@@ -223,7 +228,8 @@ def run_gpu(args):
                                    % (args.n_cells, args.degree),
                        "degree": args.degree, "n_cells": args.n_cells ** 3, "n_dofs": n, "precision": args.precision,
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "inputs larger than L2 (src+dst %.0f MB > 129 MB)" % (bytes_per_apply / 1e6)},
+                       "l2": "inputs larger than L2 (src+dst %.0f MB > 129 MB)" % (bytes_per_apply / 1e6),
+                       "launch_config": launch_config, "tuning_ms": {str(v): t for v, t in tuning}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
                          "frac": achieved / pk.get("hbm_gbs", 6800.0), "traffic": None,
                          "note": "algorithmic bytes = 2 x %d B x n_dofs per apply (src read + dst write)" % esize},
@@ -413,6 +419,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--n-cells", type=int, default=N_CELLS, help="cells per direction (profiling runs use smaller meshes)")
     ap.add_argument("--degree", type=int, default=DEGREE)
+    ap.add_argument("--no-tune", action="store_true")
+    ap.add_argument("--launch-config", type=int, default=None, help="force a launch variant (profiling)")
     ap.add_argument("--mode", default="apply", choices=["apply", "solve", "sweep", "learned"])
     ap.add_argument("--learned-steps", type=int, default=400)
     ap.add_argument("--learned-epochs", type=int, default=40)

@@ -18,6 +18,9 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relax
           "-I", SRC, "-I", os.path.join(HERE, "..", "include")]
 
 SOURCES = [
+    "sipg_cart_f64.cu",
+    "sipg_cart_f32.cu",
+    "sipg_cart_df64.cu",
     "sipg_cartesian.cu",
     "sipg_general.cu",
     "solver_kernels.cu",

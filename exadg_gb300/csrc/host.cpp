@@ -386,6 +386,7 @@ exg_mg::exg_mg(const exg_op& fine, const exg_mg_desc& d) : desc(d) {
     }
     L.op.reset(new exg_op(m, L.degree, fine.ip, prec));
     L.n = L.op->n_dofs();
+    if (L.op->cartesian && l > 0) L.op->tune(1, s, nullptr);  // autotuned launch variant per level
     size_t bytes = L.n * psize(prec);
     L.sol = dalloc(bytes);
     L.def = dalloc(bytes);

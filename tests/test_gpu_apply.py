@@ -116,3 +116,26 @@ def test_apply_large_mesh_properties():
     assert torch.linalg.norm(Aab - 2.0 * Aa - Ab) <= 1e-12 * torch.linalg.norm(Aab)
     assert abs(float(a @ Ab - b @ Aa)) <= 1e-12 * float(torch.linalg.norm(a) * torch.linalg.norm(Ab))
     assert float(a @ Aa) > 0
+
+
+@pytest.mark.parametrize("prec", [E.PREC_F64, E.PREC_F32, E.PREC_F64E])
+@pytest.mark.parametrize("kind", ["mixed", "periodic", "partial_periodic", "anisotropic"])
+@pytest.mark.parametrize("k", [1, 2, 4, 7, 8])
+def test_apply_every_launch_variant(prec, kind, k):
+    """Every launch variant the autotuner can pick (cells in a row, bricks with shared-memory halo;
+    partial bricks and periodic wrap inside a brick included) gives the oracle's result."""
+    torch = require_gpu()
+    p, m, op = pair(kind, 3, k, prec)
+    dt = torch.float32 if prec == E.PREC_F32 else torch.float64
+    x = splitmix_uniform(p.n_dofs, 9)
+    if prec == E.PREC_F32:
+        x = x.astype(np.float32).astype(np.float64)
+    ref = p.apply(x)
+    xd = to_dev(torch, x, dt)
+    best, timings = op.tune()
+    variants = [v for v, _ in timings]
+    assert len(variants) >= 5 and best in variants
+    for v in variants:
+        op.set_launch_config(v)
+        y = op.vmult(op.initialize_dof_vector(), xd)
+        assert rel(y.cpu().numpy(), ref) <= (1e-5 if prec == E.PREC_F32 else 1e-12), v

@@ -138,6 +138,34 @@ def run_reference(args):
     return 0
 
 
+def fp64_ops_per_dof(degree):
+    """FP64 instructions per DoF of the affine apply kernel for an interior cell (N = k+1):
+    3 line operators (N^2 + 4N + 8 per line), 5 mass sweeps (N^2 per line), the final sum (N per
+    line), N^2 lines per direction -> 8N + 13 + 24/N (csrc/sipg_cartesian.cuh)."""
+    n = degree + 1
+    return 8 * n + 13 + 24.0 / n
+
+
+def time_applies(op, x, y, steps, warmup, stream):
+    import torch
+
+    for _ in range(warmup):
+        op.vmult(y, x)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        op.vmult(y, x)
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+# DRAM bytes per launch measured by ncu on the 48^3 case (profiles/cart_apply_k4_48cubed.md), scaled
+# to 64^3 by the DoF count (traffic grows in proportion to the cells processed)
+NCU_TRAFFIC_48 = {"f64": (110.78e6 + 82.77e6), "f32": (55.33e6 + 35.86e6), "f64e": (111.01e6 + 80.01e6)}
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -153,22 +181,30 @@ def run_gpu(args):
         dist.init_process_group("nccl")
     B.build()
     E.load_library()
-    prec = {"f64": E.PREC_F64, "f32": E.PREC_F32, "f64e": E.PREC_F64E}[args.precision]
+    precs = {"f64": E.PREC_F64, "f32": E.PREC_F32, "f64e": E.PREC_F64E}
+    prec = precs[args.precision]
     mesh = E.Mesh(args.n_cells)
-    op = E.LaplaceOperator(mesh, args.degree, 1.0, prec)
-    if args.launch_config is not None:
-        op.set_launch_config(args.launch_config)
-        launch_config, tuning = args.launch_config, []
-    else:
-        launch_config, tuning = op.tune() if not args.no_tune else (0, [])
+    stream = torch.cuda.current_stream()
+
+    def make(pname):
+        op = E.LaplaceOperator(mesh, args.degree, 1.0, precs[pname])
+        if args.launch_config is not None:
+            op.set_launch_config(args.launch_config)
+            return op, args.launch_config, []
+        if args.no_tune:
+            return op, 0, []
+        best, tuning = op.tune()
+        return op, best, tuning
+
+    op, launch_config, tuning = make(args.precision)
     n = op.n_dofs
     dt = op.dtype
     esize = 4 if prec == E.PREC_F32 else 8
-    x_host = torch.tensor(splitmix_uniform(n, 1 + rank), dtype=dt).pin_memory()
+    x64 = torch.tensor(splitmix_uniform(n, 1 + rank), dtype=torch.float64)
+    x_host = x64.to(dt).pin_memory()
     y_host = torch.empty(n, dtype=dt).pin_memory()
     x = x_host.to("cuda")
     y = torch.empty_like(x)
-    stream = torch.cuda.current_stream()
 
     def barrier():
         if world > 1:
@@ -195,6 +231,7 @@ def run_gpu(args):
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         ms = float(t.item())
     value = world * n / (ms * 1e-3)
+    y_ref = y.double().clone()
 
     # e2e: host input -> device -> apply -> host output, every step
     for _ in range(2):
@@ -218,27 +255,70 @@ def run_gpu(args):
     achieved = bytes_per_apply / (ms * 1e-3) / 1e9
     out = None
     if rank == 0:
-        cb = cpu_apply_sample(seconds=10.0) if not args.no_cpu_baseline else None
-        out = {
+        f64_tf, f32_tf = E.device_fma_peaks()
+        traffic = NCU_TRAFFIC_48.get(args.precision) if args.degree == DEGREE else None
+        if traffic is not None:
+            traffic *= n / 13824000.0
+        line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": {"f64": "f64", "f32": "f32", "f64e": "f64 (FP32-pair arithmetic)"}[args.precision],
-            "data": "synthetic",
+            "vs_baseline": None, "dtype": {"f64": "f64", "f32": "f32", "f64e": "f32x2 (double-float)"}[args.precision],
+            "data": "synthetic (SplitMix64 uniform[-1,1] input)",
             "config": {"workload": "SIPG Laplace apply, Cartesian %d^3 cells of [0,1]^3, all Dirichlet, k=%d"
                                    % (args.n_cells, args.degree),
                        "degree": args.degree, "n_cells": args.n_cells ** 3, "n_dofs": n, "precision": args.precision,
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "inputs larger than L2 (src+dst %.0f MB > 129 MB)" % (bytes_per_apply / 1e6),
+                       "l2": "inputs larger than L2 (src+dst %.0f MB > 129 MB), no flush" % (bytes_per_apply / 1e6),
                        "launch_config": launch_config, "tuning_ms": {str(v): t for v, t in tuning}},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": pk.get("hbm_gbs"), "unit": "GB/s",
-                         "frac": achieved / pk.get("hbm_gbs", 6800.0), "traffic": None,
-                         "note": "algorithmic bytes = 2 x %d B x n_dofs per apply (src read + dst write)" % esize},
-            "cpu_baseline": cb,
+                         "frac": achieved / pk.get("hbm_gbs", 6800.0),
+                         "traffic": traffic,
+                         "note": "of measured; algorithmic bytes = 2 x %d B x n_dofs per apply; traffic = ncu DRAM "
+                                 "read+write of the 48^3 capture scaled by DoF" % esize},
             "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": esize * n,
                     "d2h_bytes_per_step": esize * n},
             "gpu_launches": args.steps,
             "clocks": clk.summary(),
+            "device_fma_peaks_tflops": {"f64": f64_tf, "f32": f32_tf},
         }
+        if args.precision == "f64":
+            ops = fp64_ops_per_dof(args.degree)
+            line["compute_roofline"] = {"bound": "fp64 pipe (GB300 FP64 is 1/60 of FP32)", "ops_per_dof": ops,
+                                        "achieved_tops": value * ops / 1e12,
+                                        "peak_tops": f64_tf / 2,
+                                        "unit": "T FP64 instructions/s",
+                                        "frac": value * ops / (f64_tf * 1e12 / 2),
+                                        "note": "FP64 instructions per DoF counted from the kernel; peak = measured "
+                                                "FP64 FMA rate; an FMA counts as one instruction"}
+        if not args.no_variants and args.n_cells == N_CELLS:
+            variants = {}
+            for pname in ("f64", "f64e", "f32"):
+                if pname == args.precision:
+                    continue
+                vop, vcfg, _ = make(pname)
+                vx = x64.to(vop.dtype).cuda()
+                vy = torch.empty_like(vx)
+                vms = time_applies(vop, vx, vy, max(10, args.steps // 2), 3, stream)
+                vesize = 4 if pname == "f32" else 8
+                diff = float(torch.linalg.norm(vy.double() - y_ref) / torch.linalg.norm(y_ref))
+                variants[pname] = {"value": n / (vms * 1e-3), "ms_per_step": vms, "launch_config": vcfg,
+                                   "rel_l2_diff_vs_headline": diff,
+                                   "hbm_frac": 2.0 * vesize * n / (vms * 1e-3) / 1e9 / pk.get("hbm_gbs", 6800.0)}
+                del vop, vx, vy
+            line["variants"] = variants
+        if not args.no_solve and args.n_cells == N_CELLS:
+            from exadg_gb300 import driver as D
+
+            x64s, r64 = D.solve_unit_cube_sine(N_CELLS, DEGREE, E.PREC_F64, E.PREC_F64)
+            xm, rm = D.solve_unit_cube_sine(N_CELLS, DEGREE, E.PREC_F64E, E.PREC_F32)
+            line["solve_to_1e-10"] = {
+                "plain_fp64": {"iterations": r64["iterations"], "seconds": r64["wall_seconds"]},
+                "mixed_fp32_graph_vcycle": {"iterations": rm["iterations"], "seconds": rm["wall_seconds"]},
+                "speedup": r64["wall_seconds"] / rm["wall_seconds"],
+                "solution_rel_diff": float(torch.linalg.norm(xm - x64s) / torch.linalg.norm(x64s))}
+            del x64s, xm
+        line["cpu_baseline"] = cpu_apply_sample(seconds=10.0) if not args.no_cpu_baseline else None
+        out = line
         print(json.dumps(out))
     if world > 1:
         import torch.distributed as dist
@@ -421,6 +501,8 @@ def main():
     ap.add_argument("--degree", type=int, default=DEGREE)
     ap.add_argument("--no-tune", action="store_true")
     ap.add_argument("--launch-config", type=int, default=None, help="force a launch variant (profiling)")
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--mode", default="apply", choices=["apply", "solve", "sweep", "learned"])
     ap.add_argument("--learned-steps", type=int, default=400)
     ap.add_argument("--learned-epochs", type=int, default=40)

@@ -112,7 +112,7 @@ EXPORTED_SYMBOLS = [
     "exg_sipg_info", "exg_sipg_tune", "exg_sipg_set_launch_config", "exg_sipg_apply_f64", "exg_sipg_apply_f32", "exg_sipg_inverse_diagonal_f64",
     "exg_sipg_inverse_diagonal_f32", "exg_sipg_quadrature_points", "exg_sipg_rhs", "exg_mg_default_desc",
     "exg_mg_create", "exg_mg_destroy", "exg_mg_vmult", "exg_mg_info_get", "exg_cg_default_desc", "exg_cg_solve",
-    "exg_cg_solve_noalloc", "exg_status_string", "exg_last_error",
+    "exg_cg_solve_noalloc", "exg_device_fma_peaks", "exg_status_string", "exg_last_error",
     "exg_cnn_create", "exg_cnn_destroy", "exg_cnn_n_params", "exg_cnn_params", "exg_cnn_forward",
     "exg_cnn_backward", "exg_cnn_train_step", "exg_cnn_adam", "exg_dg_pack", "exg_dg_unpack_add", "exg_dg_pack_diff",
 ]
@@ -156,6 +156,7 @@ def load_library(path=LIB_PATH):
         "exg_cg_default_desc": [ctypes.POINTER(CGDesc)],
         "exg_cg_solve": [P, P, ctypes.POINTER(CGDesc), P, P, ctypes.POINTER(CGResult), P],
         "exg_cg_solve_noalloc": [P, ctypes.POINTER(CGDesc), P, P, ctypes.POINTER(CGResult), P],
+        "exg_device_fma_peaks": [ctypes.POINTER(D), ctypes.POINTER(D), P],
         "exg_cnn_create": [ctypes.POINTER(I), I, I, I, ctypes.c_ulonglong, PP],
         "exg_cnn_destroy": [P],
         "exg_cnn_n_params": [P, ctypes.POINTER(LL)],
@@ -203,6 +204,14 @@ def _stream(stream=None):
 
     s = stream if stream is not None else torch.cuda.current_stream()
     return ctypes.c_void_p(s.cuda_stream)
+
+
+def device_fma_peaks(stream=None):
+    """(FP64, FP32) FMA throughput of the current device in TFLOP/s, measured."""
+    f64 = ctypes.c_double()
+    f32 = ctypes.c_double()
+    _check(load_library().exg_device_fma_peaks(ctypes.byref(f64), ctypes.byref(f32), _stream(stream)))
+    return f64.value, f32.value
 
 
 class Mesh:

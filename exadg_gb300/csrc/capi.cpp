@@ -48,6 +48,12 @@ const char* exg_status_string(exg_status s) {
 
 const char* exg_last_error(void) { return g_last_error.c_str(); }
 
+exg_status exg_device_fma_peaks(double* f64_tflops, double* f32_tflops, void* stream) {
+  EXG_API_BEGIN
+  device_fma_peaks(f64_tflops, f32_tflops, (cudaStream_t)stream);
+  EXG_API_END
+}
+
 exg_status exg_mesh_create(const exg_mesh_desc* desc, exg_mesh** mesh) {
   EXG_API_BEGIN
   EXG_CHECK(desc && mesh, EXG_ERR_INVALID, "null argument");

@@ -100,5 +100,6 @@ std::vector<int> cart_cpb_options(int n, int precision);
 // ------------------------------------------------------------------------------------------
 void vec_copy_convert(const void* src, int src_prec, void* dst, int dst_prec, long long n, cudaStream_t s);
 void vec_fill(void* x, int prec, double v, long long n, cudaStream_t s);
+void device_fma_peaks(double* f64_tflops, double* f32_tflops, cudaStream_t s);
 
 }  // namespace exg

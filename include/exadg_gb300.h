@@ -208,6 +208,10 @@ exg_status exg_dg_pack_diff(const double* a, const double* b, double inv_scale, 
 exg_status exg_cg_solve_noalloc(exg_op* op, const exg_cg_desc* desc, const double* b, double* x,
                                 exg_cg_result* result, void* stream);
 
+/* Measured FMA throughput of the current device (TFLOP/s, FMA = 2 flops) for the compute-side
+ * roofline of the operator kernels.  No reference counterpart. */
+exg_status exg_device_fma_peaks(double* f64_tflops, double* f32_tflops, void* stream);
+
 const char* exg_status_string(exg_status status);
 const char* exg_last_error(void);
 

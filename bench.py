@@ -139,11 +139,14 @@ def run_reference(args):
 
 
 def fp64_ops_per_dof(degree):
-    """FP64 instructions per DoF of the affine apply kernel for an interior cell (N = k+1):
-    3 line operators (N^2 + 4N + 8 per line), 5 mass sweeps (N^2 per line), the final sum (N per
-    line), N^2 lines per direction -> 8N + 13 + 24/N (csrc/sipg_cartesian.cuh)."""
+    """FP64 instructions per DoF of the affine apply kernel for an interior cell (N = k+1), counted
+    from csrc/sipg_cartesian.cuh: every 1D matvec uses the even-odd split for N > 4 (2h + h*hm + h^2 +
+    [hm] + 2h operations, h = N/2, hm = N - h) and N^2 operations otherwise; per line three line operators (matvec + 2 penalty + 4N + 6 face
+    terms), four mass sweeps and the final sweep (matvec + 2N adds); N^2 lines per direction."""
     n = degree + 1
-    return 8 * n + 13 + 24.0 / n
+    h, hm = n // 2, n - n // 2
+    eo = 2 * h + h * hm + h * h + (hm if n % 2 else 0) + 2 * h if n > 4 else n * n
+    return (8 * eo + 14 * n + 24) / n
 
 
 def time_applies(op, x, y, steps, warmup, stream):
@@ -223,14 +226,10 @@ def run_gpu(args):
             op.vmult(y, x)
         ev1.record(stream)
         barrier()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if world > 1:
-        import torch.distributed as dist
+    from exadg_gb300.replicas import job_throughput, max_over_ranks
 
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * n / (ms * 1e-3)
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps)
+    value = job_throughput(n, ms * 1e-3, world)
     y_ref = y.double().clone()
 
     # e2e: host input -> device -> apply -> host output, every step
@@ -248,7 +247,7 @@ def run_gpu(args):
         y_host.copy_(y, non_blocking=True)
     e1.record(stream)
     barrier()
-    e2e_ms = e0.elapsed_time(e1) / e2e_steps
+    e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e2e_steps)
 
     pk = peaks()
     bytes_per_apply = 2.0 * esize * n
@@ -406,7 +405,7 @@ def run_solve(args):
     if not args.skip_curved:
         nc, kc = 48, 5
         x64, r64 = D.solve_unit_cube_sine(nc, kc, E.PREC_F64, E.PREC_F64, curved=True)
-        xm, rm = D.solve_unit_cube_sine(nc, kc, E.PREC_F64, E.PREC_F32, curved=True)
+        xm, rm = D.solve_unit_cube_sine(nc, kc, E.PREC_F64E, E.PREC_F32, curved=True)
         m = E.Mesh(**D.deformed_unit_cube(nc, degree=kc))
         o64 = E.LaplaceOperator(m, kc, 1.0, E.PREC_F64)
         o32 = E.LaplaceOperator(m, kc, 1.0, E.PREC_F32)

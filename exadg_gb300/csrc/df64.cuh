@@ -98,6 +98,16 @@ __device__ __forceinline__ df64 operator+(df64 a, df64 b) {
 __device__ __forceinline__ df64 operator-(df64 a, df64 b) { return a + df64(-b.hi, -b.lo); }
 __device__ __forceinline__ df64 neg(df64 a) { return df64(-a.hi, -a.lo); }
 
+// small exactly representable constants in the compute type
+template <class C>
+__host__ __device__ inline C cconst(double v);
+template <>
+__host__ __device__ inline double cconst<double>(double v) { return v; }
+template <>
+__host__ __device__ inline float cconst<float>(double v) { return (float)v; }
+template <>
+__host__ __device__ inline df64 cconst<df64>(double v) { return df64((float)v, 0.0f); }
+
 // ---------------------------------------------------------------- loads / stores
 template <class C, class T>
 __device__ __forceinline__ C load_as(const T* p);

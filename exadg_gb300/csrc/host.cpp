@@ -61,7 +61,6 @@ exg_op::exg_op(const MeshInfo& m, int deg, double ip_factor, int prec)
   cartesian = m.affine();
   build_cart_host(m, fe, ip, cart);
   if (!cartesian) {
-    EXG_CHECK(prec != EXG_PREC_F64E, EXG_ERR_UNSUPPORTED, "FP64-emulated arithmetic is implemented for affine meshes");
     geo.reset(new GeneralGeom());
     geo->build(m, fe, ip, prec, false, nullptr);
     EXG_CUDA(cudaDeviceSynchronize());

@@ -26,13 +26,82 @@
 
 namespace exg {
 
+// even-odd split of a centrosymmetric N x N matrix A (A[i][j] = A[N-1-i][N-1-j]), h = N/2:
+//   e_j = x_j + x_{N-1-j}, o_j = x_j - x_{N-1-j} (j < h), middle x_h for odd N
+//   y_i = ye_i + yo_i, y_{N-1-i} = ye_i - yo_i (i < h), y_h = sum_j Mid_j e_j + Mid_h x_h (odd N)
+//   ye_i = sum_{j<h} E_ij e_j (+ E_ih x_h), yo_i = sum_{j<h} O_ij o_j
+//   E_ij = (A_ij + A_i,N-1-j)/2, O_ij = (A_ij - A_i,N-1-j)/2
+template <int N>
+struct EO {
+  static constexpr int h = N / 2, hm = N - N / 2;
+};
+
 template <int N, class C>
 struct CartCoef {
   C M[N * N];
   C B[3][N * N];
   C sdL[3][N], sdR[3][N];
   C tauA[3][64];  // A_d * tau_c * (k+1)^2 IP per cell boundary class
+  C Me[EO<N>::h * EO<N>::hm], Mo[EO<N>::h * EO<N>::h + 1], Mm[EO<N>::hm];
+  C Be[3][EO<N>::h * EO<N>::hm], Bo[3][EO<N>::h * EO<N>::h + 1], Bm[3][EO<N>::hm];
 };
+
+template <int N, class C>
+static void split_eo(const double* A, C* E, C* O, C* Mid) {
+  constexpr int h = EO<N>::h, hm = EO<N>::hm;
+  for (int i = 0; i < h; ++i) {
+    for (int j = 0; j < h; ++j) {
+      E[i * hm + j] = coef_from_double<C>(0.5 * (A[i * N + j] + A[i * N + N - 1 - j]));
+      O[i * h + j] = coef_from_double<C>(0.5 * (A[i * N + j] - A[i * N + N - 1 - j]));
+    }
+    if (N % 2) E[i * hm + h] = coef_from_double<C>(A[i * N + h]);
+  }
+  if (N % 2) {
+    for (int j = 0; j < h; ++j) Mid[j] = coef_from_double<C>(A[h * N + j]);
+    Mid[h] = coef_from_double<C>(A[h * N + h]);
+  }
+}
+
+// y = A x for a centrosymmetric A: plain for N <= 4 (the split saves nothing there), even-odd above
+template <int N, class C>
+__device__ __forceinline__ void eo_matvec(const C* __restrict__ A, const C* __restrict__ E, const C* __restrict__ O,
+                                          const C* __restrict__ Mid, const C (&x)[N], C (&y)[N]) {
+  if constexpr (N <= 4) {
+#pragma unroll
+    for (int i = 0; i < N; ++i) {
+      C acc = A[i * N] * x[0];
+#pragma unroll
+      for (int j = 1; j < N; ++j) acc = fmadd(A[i * N + j], x[j], acc);
+      y[i] = acc;
+    }
+    return;
+  }
+  constexpr int h = EO<N>::h, hm = EO<N>::hm;
+  C e[h > 0 ? h : 1], o[h > 0 ? h : 1];
+#pragma unroll
+  for (int j = 0; j < h; ++j) {
+    e[j] = x[j] + x[N - 1 - j];
+    o[j] = x[j] - x[N - 1 - j];
+  }
+#pragma unroll
+  for (int i = 0; i < h; ++i) {
+    C ye = E[i * hm] * e[0];
+#pragma unroll
+    for (int j = 1; j < h; ++j) ye = fmadd(E[i * hm + j], e[j], ye);
+    if (N % 2) ye = fmadd(E[i * hm + h], x[h], ye);
+    C yo = O[i * h] * o[0];
+#pragma unroll
+    for (int j = 1; j < h; ++j) yo = fmadd(O[i * h + j], o[j], yo);
+    y[i] = ye + yo;
+    y[N - 1 - i] = ye - yo;
+  }
+  if (N % 2) {
+    C ym = Mid[h] * x[h];
+#pragma unroll
+    for (int j = 0; j < h; ++j) ym = fmadd(Mid[j], e[j], ym);
+    y[h] = ym;
+  }
+}
 
 template <int N, class C>
 static CartCoef<N, C> make_coef(const CartHost& h) {
@@ -45,7 +114,9 @@ static CartCoef<N, C> make_coef(const CartHost& h) {
       c.sdR[d][i] = coef_from_double<C>(h.sdR[d][i]);
     }
     for (int cls = 0; cls < 64; ++cls) c.tauA[d][cls] = coef_from_double<C>(h.tauA[d][cls]);
+    split_eo<N, C>(h.B[d], c.Be[d], c.Bo[d], c.Bm[d]);
   }
+  split_eo<N, C>(h.M, c.Me, c.Mo, c.Mm);
   return c;
 }
 
@@ -136,13 +207,7 @@ __device__ __forceinline__ void line_operator(const C* __restrict__ su, C* __res
   C u[N], w[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) u[i] = su[line_index<D, N>(i, a, b)];
-#pragma unroll
-  for (int i = 0; i < N; ++i) {
-    C acc = P.B[D][i * N] * u[0];
-#pragma unroll
-    for (int j = 1; j < N; ++j) acc = fmadd(P.B[D][i * N + j], u[j], acc);
-    w[i] = acc;
-  }
+  eo_matvec<N, C>(P.B[D], P.Be[D], P.Bo[D], P.Bm[D], u, w);
   const C tL = atau[2 * D], tR = atau[2 * D + 1];
   w[0] = fmadd(tL, u[0], w[0]);
   w[N - 1] = fmadd(tR, u[N - 1], w[N - 1]);
@@ -200,16 +265,12 @@ __device__ __forceinline__ void line_operator(const C* __restrict__ su, C* __res
 // in-place 1D mass sweep along direction D on the line (a, b); optional second array
 template <int D, int N, class C>
 __device__ __forceinline__ void mass_line(C* __restrict__ x, int a, int b, const CartCoef<N, C>& P) {
-  C v[N];
+  C v[N], r[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) v[i] = x[line_index<D, N>(i, a, b)];
+  eo_matvec<N, C>(P.M, P.Me, P.Mo, P.Mm, v, r);
 #pragma unroll
-  for (int i = 0; i < N; ++i) {
-    C acc = P.M[i * N] * v[0];
-#pragma unroll
-    for (int j = 1; j < N; ++j) acc = fmadd(P.M[i * N + j], v[j], acc);
-    x[line_index<D, N>(i, a, b)] = acc;
-  }
+  for (int i = 0; i < N; ++i) x[line_index<D, N>(i, a, b)] = r[i];
 }
 
 template <int N, int CPB, class T, class C>
@@ -276,13 +337,12 @@ __global__ void __launch_bounds__(CPB* N* N) cart_apply_kernel(const T* __restri
       v[k] = wx[co + id] + wy[co + id];
     }
     T* oc = o + base + co;
+    C r[N];
+    eo_matvec<N, C>(P.M, P.Me, P.Mo, P.Mm, v, r);
 #pragma unroll
     for (int k = 0; k < N; ++k) {
       int id = line_index<2, N>(k, a, b);
-      C acc = wz[co + id];
-#pragma unroll
-      for (int j = 0; j < N; ++j) acc = fmadd(P.M[k * N + j], v[j], acc);
-      store_as<T>(oc + id, acc);
+      store_as<T>(oc + id, r[k] + wz[co + id]);
     }
   }
 }
@@ -316,13 +376,7 @@ __device__ __forceinline__ void line_operator_s(const C* __restrict__ su, C* __r
   C u[N], w[N];
 #pragma unroll
   for (int i = 0; i < N; ++i) u[i] = su[line_index<D, N>(i, a, b)];
-#pragma unroll
-  for (int i = 0; i < N; ++i) {
-    C acc = P.B[D][i * N] * u[0];
-#pragma unroll
-    for (int j = 1; j < N; ++j) acc = fmadd(P.B[D][i * N + j], u[j], acc);
-    w[i] = acc;
-  }
+  eo_matvec<N, C>(P.B[D], P.Be[D], P.Bo[D], P.Bm[D], u, w);
   w[0] = fmadd(tL, u[0], w[0]);
   w[N - 1] = fmadd(tR, u[N - 1], w[N - 1]);
   if (kL == 0) {
@@ -531,13 +585,12 @@ __global__ void __launch_bounds__(BX* BY* BZ* N* N)
     }
     const long long gc = (long long)(x0[0] + lx) + (long long)m.N[0] * ((x0[1] + ly) + (long long)m.N[1] * (x0[2] + lz));
     T* oc = o + gc * N3;
+    C r[N];
+    eo_matvec<N, C>(P.M, P.Me, P.Mo, P.Mm, v, r);
 #pragma unroll
     for (int k = 0; k < N; ++k) {
       int id = line_index<2, N>(k, a, b);
-      C acc = wz[co + id];
-#pragma unroll
-      for (int j = 0; j < N; ++j) acc = fmadd(P.M[k * N + j], v[j], acc);
-      store_as<T>(oc + id, acc);
+      store_as<T>(oc + id, r[k] + wz[co + id]);
     }
   }
 }

@@ -221,7 +221,7 @@ __global__ void geom_final_kernel(MapParams P, long long n_cells, double factor,
   int p = (int)(g - c * per);
   if (p < nq3) {
     const double* r = cell_raw + (c * nq3 + p) * 10;
-    for (int k = 0; k < 6; ++k) cellG[(c * nq3 + p) * 6 + k] = (T)r[k];
+    for (int k = 0; k < 6; ++k) cellG[(c * nq3 + p) * 6 + k] = coef_from_double<T>(r[k]);
     return;
   }
   int rr = p - nq3;
@@ -238,13 +238,13 @@ __global__ void geom_final_kernel(MapParams P, long long n_cells, double factor,
   const double* nrm = rm + 9;
   T* o = face + ((c * 6 + f) * nq2 + q) * 7;
   for (int i = 0; i < 3; ++i) {
-    o[i] = (T)(ro[i * 3 + 0] * nrm[0] + ro[i * 3 + 1] * nrm[1] + ro[i * 3 + 2] * nrm[2]);
-    o[3 + i] = rn ? (T)(rn[i * 3 + 0] * nrm[0] + rn[i * 3 + 1] * nrm[1] + rn[i * 3 + 2] * nrm[2]) : (T)0;
+    o[i] = coef_from_double<T>(ro[i * 3 + 0] * nrm[0] + ro[i * 3 + 1] * nrm[1] + ro[i * 3 + 2] * nrm[2]);
+    o[3 + i] = coef_from_double<T>(rn ? rn[i * 3 + 0] * nrm[0] + rn[i * 3 + 1] * nrm[1] + rn[i * 3 + 2] * nrm[2] : 0.0);
   }
-  o[6] = (T)rm[12];
+  o[6] = coef_from_double<T>(rm[12]);
   if (q == 0) {
     double t = nb >= 0 ? fmax(tau[c], tau[nb]) * factor : tau[c] * factor;
-    ftau[c * 6 + f] = (T)t;
+    ftau[c * 6 + f] = coef_from_double<T>(t);
     // encoding: >= 0 neighbour cell; -1 Dirichlet; -2 Neumann
     fnb[c * 6 + f] = nb >= 0 ? nb : (bc[f] == EXG_BC_DIRICHLET ? -1 : -2);
   }
@@ -306,6 +306,9 @@ void GeneralGeom::build(const MeshInfo& m, const FE1D& fe, double ip, int prec, 
   if (prec == EXG_PREC_F32)
     geom_final_kernel<float><<<(unsigned)((total + 127) / 128), 128, 0, s>>>(
         P, n_cells, factor, bc_dev, cell_raw, face_raw, tau, (float*)cellG, (float*)face, (float*)ftau, fnb);
+  else if (prec == EXG_PREC_F64E)
+    geom_final_kernel<df64><<<(unsigned)((total + 127) / 128), 128, 0, s>>>(
+        P, n_cells, factor, bc_dev, cell_raw, face_raw, tau, (df64*)cellG, (df64*)face, (df64*)ftau, fnb);
   else
     geom_final_kernel<double><<<(unsigned)((total + 127) / 128), 128, 0, s>>>(
         P, n_cells, factor, bc_dev, cell_raw, face_raw, tau, (double*)cellG, (double*)face, (double*)ftau, fnb);
@@ -337,21 +340,21 @@ __device__ __forceinline__ int fidx(int N, int d, int i, int p1, int p2) {
   return d == 0 ? i + N * (p1 + N * p2) : (d == 1 ? p1 + N * (i + N * p2) : p1 + N * (p2 + N * i));
 }
 
-template <int N, int CPB, class T>
+template <int N, int CPB, class T, class C>
 __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restrict__ src, T* __restrict__ dst,
-                                                              const __grid_constant__ GenCoef<N, T> P,
-                                                              const T* __restrict__ cellG, const T* __restrict__ face,
-                                                              const T* __restrict__ ftau,
+                                                              const __grid_constant__ GenCoef<N, C> P,
+                                                              const C* __restrict__ cellG, const C* __restrict__ face,
+                                                              const C* __restrict__ ftau,
                                                               const long long* __restrict__ fnb, long long n_cells,
                                                               long long n_dofs) {
   constexpr int N2 = N * N, N3 = N2 * N, NT = CPB * N2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* su = reinterpret_cast<T*>(smem_raw);
-  T* so = su + CPB * N3;
-  T* t0 = so + CPB * N3;
-  T* t1 = t0 + CPB * N3;
-  T* t2 = t1 + CPB * N3;
-  T* fsh = t2 + CPB * N3;  // CPB * 16 * N2 face scratch
+  C* su = reinterpret_cast<C*>(smem_raw);
+  C* so = su + CPB * N3;
+  C* t0 = so + CPB * N3;
+  C* t1 = t0 + CPB * N3;
+  C* t2 = t1 + CPB * N3;
+  C* fsh = t2 + CPB * N3;  // CPB * 16 * N2 face scratch
 
   const long long c0 = (long long)blockIdx.x * CPB;
   const T* s = src + (long long)blockIdx.y * n_dofs;
@@ -361,30 +364,30 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
   const long long nch = min((long long)CPB, n_cells - c0);
   const int nd = (int)(nch * N3);
   for (int i = tid; i < CPB * N3; i += NT) {
-    su[i] = i < nd ? s[base + i] : T(0);
-    so[i] = T(0);
+    su[i] = i < nd ? load_as<C>(s + base + i) : C(0);
+    so[i] = C(0);
   }
   __syncthreads();
   const int lc = tid / N2, l = tid - lc * N2, a = l % N, b = l / N;
   const bool active = lc < nch;
   const long long c = c0 + lc;
   const int co = lc * N3;
-  T* U = su + co;
-  T* A0 = t0 + co;
-  T* A1 = t1 + co;
-  T* A2 = t2 + co;
+  C* U = su + co;
+  C* A0 = t0 + co;
+  C* A1 = t1 + co;
+  C* A2 = t2 + co;
   // ---- cell term: gradients at q (x, then y, then z), G, transpose back
   if (active) {  // x-lines (j=a, k=b)
-    T u[N];
+    C u[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) u[i] = U[lidx<0, N>(i, a, b)];
 #pragma unroll
     for (int q = 0; q < N; ++q) {
-      T vs = 0, vd = 0;
+      C vs = C(0), vd = C(0);
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        vs = fma(P.S[q * N + i], u[i], vs);
-        vd = fma(P.D[q * N + i], u[i], vd);
+        vs = fmadd(P.S[q * N + i], u[i], vs);
+        vd = fmadd(P.D[q * N + i], u[i], vd);
       }
       A0[lidx<0, N>(q, a, b)] = vs;  // A = S_x u
       A1[lidx<0, N>(q, a, b)] = vd;  // B = D_x u
@@ -392,7 +395,7 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
   }
   __syncthreads();
   if (active) {  // y-lines (i=a, k=b): C = S_y A, E = D_y A, F = S_y B
-    T va[N], vb[N];
+    C va[N], vb[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       va[i] = A0[lidx<1, N>(i, a, b)];
@@ -400,12 +403,12 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
     }
 #pragma unroll
     for (int q = 0; q < N; ++q) {
-      T cs = 0, ce = 0, cf = 0;
+      C cs = C(0), ce = C(0), cf = 0;
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        cs = fma(P.S[q * N + i], va[i], cs);
-        ce = fma(P.D[q * N + i], va[i], ce);
-        cf = fma(P.S[q * N + i], vb[i], cf);
+        cs = fmadd(P.S[q * N + i], va[i], cs);
+        ce = fmadd(P.D[q * N + i], va[i], ce);
+        cf = fmadd(P.S[q * N + i], vb[i], cf);
       }
       A0[lidx<1, N>(q, a, b)] = cs;
       A1[lidx<1, N>(q, a, b)] = ce;
@@ -414,37 +417,37 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
   }
   __syncthreads();
   if (active) {  // z-lines (i=a, j=b): g2 = D_z C, g1 = S_z E, g0 = S_z F; flux; transpose
-    T vc[N], ve[N], vf[N];
+    C vc[N], ve[N], vf[N];
 #pragma unroll
     for (int i = 0; i < N; ++i) {
       vc[i] = A0[lidx<2, N>(i, a, b)];
       ve[i] = A1[lidx<2, N>(i, a, b)];
       vf[i] = A2[lidx<2, N>(i, a, b)];
     }
-    T f0[N], f1[N], f2[N];
+    C f0[N], f1[N], f2[N];
 #pragma unroll
     for (int q = 0; q < N; ++q) {
-      T g0 = 0, g1 = 0, g2 = 0;
+      C g0 = C(0), g1 = C(0), g2 = 0;
 #pragma unroll
       for (int i = 0; i < N; ++i) {
-        g0 = fma(P.S[q * N + i], vf[i], g0);
-        g1 = fma(P.S[q * N + i], ve[i], g1);
-        g2 = fma(P.D[q * N + i], vc[i], g2);
+        g0 = fmadd(P.S[q * N + i], vf[i], g0);
+        g1 = fmadd(P.S[q * N + i], ve[i], g1);
+        g2 = fmadd(P.D[q * N + i], vc[i], g2);
       }
-      const T* G = cellG + (c * N3 + lidx<2, N>(q, a, b)) * 6;
-      T G00 = G[0], G01 = G[1], G02 = G[2], G11 = G[3], G12 = G[4], G22 = G[5];
+      const C* G = cellG + (c * N3 + lidx<2, N>(q, a, b)) * 6;
+      C G00 = G[0], G01 = G[1], G02 = G[2], G11 = G[3], G12 = G[4], G22 = G[5];
       f0[q] = G00 * g0 + G01 * g1 + G02 * g2;
       f1[q] = G01 * g0 + G11 * g1 + G12 * g2;
       f2[q] = G02 * g0 + G12 * g1 + G22 * g2;
     }
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      T xf = 0, xe = 0, xc = 0;
+      C xf = C(0), xe = C(0), xc = 0;
 #pragma unroll
       for (int q = 0; q < N; ++q) {
-        xf = fma(P.S[q * N + i], f0[q], xf);
-        xe = fma(P.S[q * N + i], f1[q], xe);
-        xc = fma(P.D[q * N + i], f2[q], xc);
+        xf = fmadd(P.S[q * N + i], f0[q], xf);
+        xe = fmadd(P.S[q * N + i], f1[q], xe);
+        xc = fmadd(P.D[q * N + i], f2[q], xc);
       }
       A2[lidx<2, N>(i, a, b)] = xf;  // F'
       A1[lidx<2, N>(i, a, b)] = xe;  // E'
@@ -453,7 +456,7 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
   }
   __syncthreads();
   if (active) {  // y-lines: A' = S^T C' + D^T E', B' = S^T F'
-    T vc[N], ve[N], vf[N];
+    C vc[N], ve[N], vf[N];
 #pragma unroll
     for (int q = 0; q < N; ++q) {
       vc[q] = A0[lidx<1, N>(q, a, b)];
@@ -462,12 +465,12 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
     }
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      T xa = 0, xb = 0;
+      C xa = C(0), xb = C(0);
 #pragma unroll
       for (int q = 0; q < N; ++q) {
-        xa = fma(P.S[q * N + i], vc[q], xa);
-        xa = fma(P.D[q * N + i], ve[q], xa);
-        xb = fma(P.S[q * N + i], vf[q], xb);
+        xa = fmadd(P.S[q * N + i], vc[q], xa);
+        xa = fmadd(P.D[q * N + i], ve[q], xa);
+        xb = fmadd(P.S[q * N + i], vf[q], xb);
       }
       A0[lidx<1, N>(i, a, b)] = xa;
       A1[lidx<1, N>(i, a, b)] = xb;
@@ -475,7 +478,7 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
   }
   __syncthreads();
   if (active) {  // x-lines: out = S^T A' + D^T B'
-    T va[N], vb[N];
+    C va[N], vb[N];
 #pragma unroll
     for (int q = 0; q < N; ++q) {
       va[q] = A0[lidx<0, N>(q, a, b)];
@@ -483,32 +486,32 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
     }
 #pragma unroll
     for (int i = 0; i < N; ++i) {
-      T x = 0;
+      C x = C(0);
 #pragma unroll
       for (int q = 0; q < N; ++q) {
-        x = fma(P.S[q * N + i], va[q], x);
-        x = fma(P.D[q * N + i], vb[q], x);
+        x = fmadd(P.S[q * N + i], va[q], x);
+        x = fmadd(P.D[q * N + i], vb[q], x);
       }
       so[co + lidx<0, N>(i, a, b)] = x;
     }
   }
   __syncthreads();
   // ---- face terms
-  T* F = fsh + lc * 16 * N2;
-  T* fv = F;            // own trace value at face nodes
-  T* fn = F + N2;       // own normal-direction derivative at face nodes
-  T* gv = F + 2 * N2;   // neighbour trace value
-  T* gn = F + 3 * N2;   // neighbour normal derivative
-  T* r0 = F + 4 * N2;   // stage-1 buffers (q1, p2)
-  T* r1 = F + 5 * N2;
-  T* r2 = F + 6 * N2;
-  T* r3 = F + 7 * N2;
-  T* r4 = F + 8 * N2;
-  T* r5 = F + 9 * N2;
-  T* cv = F + 10 * N2;  // flux coefficients at face q
-  T* c0_ = F + 11 * N2;
-  T* c1_ = F + 12 * N2;
-  T* c2_ = F + 13 * N2;
+  C* F = fsh + lc * 16 * N2;
+  C* fv = F;            // own trace value at face nodes
+  C* fn = F + N2;       // own normal-direction derivative at face nodes
+  C* gv = F + 2 * N2;   // neighbour trace value
+  C* gn = F + 3 * N2;   // neighbour normal derivative
+  C* r0 = F + 4 * N2;   // stage-1 buffers (q1, p2)
+  C* r1 = F + 5 * N2;
+  C* r2 = F + 6 * N2;
+  C* r3 = F + 7 * N2;
+  C* r4 = F + 8 * N2;
+  C* r5 = F + 9 * N2;
+  C* cv = F + 10 * N2;  // flux coefficients at face q
+  C* c0_ = F + 11 * N2;
+  C* c1_ = F + 12 * N2;
+  C* c2_ = F + 13 * N2;
   const int p1 = a, p2 = b;  // this thread's face point / node
 #pragma unroll 1
   for (int f = 0; f < 6; ++f) {
@@ -517,35 +520,35 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
     tang(d, t1d, t2d);
     long long nb = active ? fnb[c * 6 + f] : -2;
     const bool interior = nb >= 0;
-    const T* dside = side ? P.d1 : P.d0;
-    const T* dopp = side ? P.d0 : P.d1;
+    const C* dside = side ? P.d1 : P.d0;
+    const C* dopp = side ? P.d0 : P.d1;
     const int iend = side ? N - 1 : 0, iopp = side ? 0 : N - 1;
     if (active) {
-      T nd = 0;
-      for (int i = 0; i < N; ++i) nd = fma(dside[i], U[fidx(N, d, i, p1, p2)], nd);
+      C nd = C(0);
+      for (int i = 0; i < N; ++i) nd = fmadd(dside[i], U[fidx(N, d, i, p1, p2)], nd);
       fv[p2 * N + p1] = U[fidx(N, d, iend, p1, p2)];
       fn[p2 * N + p1] = nd;
       if (interior) {
         const T* un = s + nb * N3;
-        T ndn = 0;
-        for (int i = 0; i < N; ++i) ndn = fma(dopp[i], un[fidx(N, d, i, p1, p2)], ndn);
-        gv[p2 * N + p1] = un[fidx(N, d, iopp, p1, p2)];
+        C ndn = C(0);
+        for (int i = 0; i < N; ++i) ndn = fmadd(dopp[i], load_as<C>(un + fidx(N, d, i, p1, p2)), ndn);
+        gv[p2 * N + p1] = load_as<C>(un + fidx(N, d, iopp, p1, p2));
         gn[p2 * N + p1] = ndn;
       }
     }
     __syncthreads();
     // stage 1 along t1: thread (q1 = p1, p2): contract over node index p1'
     if (active && nb != -2) {
-      T sv = 0, sdv = 0, sn = 0, nv = 0, ndv = 0, nn = 0;
+      C sv = C(0), sdv = C(0), sn = 0, nv = C(0), ndv = 0, nn = C(0);
       for (int k = 0; k < N; ++k) {
-        T Sq = P.S[p1 * N + k], Dq = P.D[p1 * N + k];
-        sv = fma(Sq, fv[p2 * N + k], sv);
-        sdv = fma(Dq, fv[p2 * N + k], sdv);
-        sn = fma(Sq, fn[p2 * N + k], sn);
+        C Sq = P.S[p1 * N + k], Dq = P.D[p1 * N + k];
+        sv = fmadd(Sq, fv[p2 * N + k], sv);
+        sdv = fmadd(Dq, fv[p2 * N + k], sdv);
+        sn = fmadd(Sq, fn[p2 * N + k], sn);
         if (interior) {
-          nv = fma(Sq, gv[p2 * N + k], nv);
-          ndv = fma(Dq, gv[p2 * N + k], ndv);
-          nn = fma(Sq, gn[p2 * N + k], nn);
+          nv = fmadd(Sq, gv[p2 * N + k], nv);
+          ndv = fmadd(Dq, gv[p2 * N + k], ndv);
+          nn = fmadd(Sq, gn[p2 * N + k], nn);
         }
       }
       r0[p2 * N + p1] = sv;
@@ -559,50 +562,50 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
     // stage 2 along t2: thread (q1 = p1, q2 = p2): values / reference gradients at the face point,
     // then the SIPG flux (laplace_operator.cpp:139-163 / 221-265)
     if (active && nb != -2) {
-      T vo = 0, go_t1 = 0, go_t2 = 0, go_d = 0, vn = 0, gn_t1 = 0, gn_t2 = 0, gn_d = 0;
+      C vo = C(0), go_t1 = C(0), go_t2 = 0, go_d = C(0), vn = 0, gn_t1 = C(0), gn_t2 = 0, gn_d = C(0);
       for (int k = 0; k < N; ++k) {
-        T Sq = P.S[p2 * N + k], Dq = P.D[p2 * N + k];
-        vo = fma(Sq, r0[k * N + p1], vo);
-        go_t2 = fma(Dq, r0[k * N + p1], go_t2);
-        go_t1 = fma(Sq, r1[k * N + p1], go_t1);
-        go_d = fma(Sq, r2[k * N + p1], go_d);
+        C Sq = P.S[p2 * N + k], Dq = P.D[p2 * N + k];
+        vo = fmadd(Sq, r0[k * N + p1], vo);
+        go_t2 = fmadd(Dq, r0[k * N + p1], go_t2);
+        go_t1 = fmadd(Sq, r1[k * N + p1], go_t1);
+        go_d = fmadd(Sq, r2[k * N + p1], go_d);
         if (interior) {
-          vn = fma(Sq, r3[k * N + p1], vn);
-          gn_t2 = fma(Dq, r3[k * N + p1], gn_t2);
-          gn_t1 = fma(Sq, r4[k * N + p1], gn_t1);
-          gn_d = fma(Sq, r5[k * N + p1], gn_d);
+          vn = fmadd(Sq, r3[k * N + p1], vn);
+          gn_t2 = fmadd(Dq, r3[k * N + p1], gn_t2);
+          gn_t1 = fmadd(Sq, r4[k * N + p1], gn_t1);
+          gn_d = fmadd(Sq, r5[k * N + p1], gn_d);
         }
       }
-      const T* fd = face + ((c * 6 + f) * N2 + p2 * N + p1) * 7;
-      T ao[3] = {fd[0], fd[1], fd[2]};
-      T JxW = fd[6];
-      T gref_o[3];
+      const C* fd = face + ((c * 6 + f) * N2 + p2 * N + p1) * 7;
+      C ao[3] = {fd[0], fd[1], fd[2]};
+      C JxW = fd[6];
+      C gref_o[3];
       gref_o[d] = go_d;
       gref_o[t1d] = go_t1;
       gref_o[t2d] = go_t2;
-      T ndo = ao[0] * gref_o[0] + ao[1] * gref_o[1] + ao[2] * gref_o[2];
-      T tau = ftau[c * 6 + f];
-      T gflux, sv;
+      C ndo = ao[0] * gref_o[0] + ao[1] * gref_o[1] + ao[2] * gref_o[2];
+      C tau = ftau[c * 6 + f];
+      C gflux, sv;
       if (interior) {
-        T an[3] = {fd[3], fd[4], fd[5]};
-        T gref_n[3];
+        C an[3] = {fd[3], fd[4], fd[5]};
+        C gref_n[3];
         gref_n[d] = gn_d;
         gref_n[t1d] = gn_t1;
         gref_n[t2d] = gn_t2;
-        T ndn = an[0] * gref_n[0] + an[1] * gref_n[1] + an[2] * gref_n[2];
+        C ndn = an[0] * gref_n[0] + an[1] * gref_n[1] + an[2] * gref_n[2];
         const bool own_minus = side == 1;
-        T um = own_minus ? vo : vn, up = own_minus ? vn : vo;
-        T nm = own_minus ? ndo : ndn, np = own_minus ? ndn : ndo;
-        gflux = T(-0.5) * (um - up);
-        T vflux = T(0.5) * (nm + np) - tau * (um - up);
-        sv = own_minus ? -vflux : vflux;
+        C um = own_minus ? vo : vn, up = own_minus ? vn : vo;
+        C nm = own_minus ? ndo : ndn, np = own_minus ? ndn : ndo;
+        gflux = cconst<C>(-0.5) * (um - up);
+        C vflux = cconst<C>(0.5) * (nm + np) - tau * (um - up);
+        sv = own_minus ? neg(vflux) : vflux;
       } else {  // homogeneous Dirichlet: u+ = -u-, du+/dn = du-/dn
-        gflux = -vo;
-        sv = -(ndo - T(2) * tau * vo);
+        gflux = neg(vo);
+        sv = neg(ndo - cconst<C>(2.0) * tau * vo);
       }
       cv[p2 * N + p1] = JxW * sv;
-      T gj = JxW * gflux;
-      T cc[3] = {gj * ao[0], gj * ao[1], gj * ao[2]};
+      C gj = JxW * gflux;
+      C cc[3] = {gj * ao[0], gj * ao[1], gj * ao[2]};
       c0_[p2 * N + p1] = cc[d];
       c1_[p2 * N + p1] = cc[t1d];
       c2_[p2 * N + p1] = cc[t2d];
@@ -610,13 +613,13 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
     __syncthreads();
     // integrate stage 1 along t2: thread (q1 = p1, node p2)
     if (active && nb != -2) {
-      T s1 = 0, s2 = 0, s3 = 0, s4 = 0;
+      C s1 = C(0), s2 = C(0), s3 = 0, s4 = C(0);
       for (int q = 0; q < N; ++q) {
-        T Sq = P.S[q * N + p2], Dq = P.D[q * N + p2];
-        s1 = fma(Sq, cv[q * N + p1], s1);
-        s2 = fma(Sq, c1_[q * N + p1], s2);
-        s3 = fma(Dq, c2_[q * N + p1], s3);
-        s4 = fma(Sq, c0_[q * N + p1], s4);
+        C Sq = P.S[q * N + p2], Dq = P.D[q * N + p2];
+        s1 = fmadd(Sq, cv[q * N + p1], s1);
+        s2 = fmadd(Sq, c1_[q * N + p1], s2);
+        s3 = fmadd(Dq, c2_[q * N + p1], s3);
+        s4 = fmadd(Sq, c0_[q * N + p1], s4);
       }
       r0[p2 * N + p1] = s1;
       r1[p2 * N + p1] = s2;
@@ -626,32 +629,32 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
     __syncthreads();
     // stage 2 along t1: thread (node p1, node p2) owns the line through it along d
     if (active && nb != -2) {
-      T tv = 0, tn = 0;
+      C tv = C(0), tn = C(0);
       for (int q = 0; q < N; ++q) {
-        T Sq = P.S[q * N + p1], Dq = P.D[q * N + p1];
-        tv = fma(Sq, r0[p2 * N + q], tv);
-        tv = fma(Dq, r1[p2 * N + q], tv);
-        tv = fma(Sq, r2[p2 * N + q], tv);
-        tn = fma(Sq, r3[p2 * N + q], tn);
+        C Sq = P.S[q * N + p1], Dq = P.D[q * N + p1];
+        tv = fmadd(Sq, r0[p2 * N + q], tv);
+        tv = fmadd(Dq, r1[p2 * N + q], tv);
+        tv = fmadd(Sq, r2[p2 * N + q], tv);
+        tn = fmadd(Sq, r3[p2 * N + q], tn);
       }
-      so[co + fidx(N, d, iend, p1, p2)] += tv;
-      for (int i = 0; i < N; ++i) so[co + fidx(N, d, i, p1, p2)] += dside[i] * tn;
+      so[co + fidx(N, d, iend, p1, p2)] = so[co + fidx(N, d, iend, p1, p2)] + tv;
+      for (int i = 0; i < N; ++i) so[co + fidx(N, d, i, p1, p2)] = fmadd(dside[i], tn, so[co + fidx(N, d, i, p1, p2)]);
     }
     __syncthreads();
   }
-  for (int i = tid; i < nd; i += NT) o[base + i] = so[i];
+  for (int i = tid; i < nd; i += NT) store_as<T>(o + base + i, so[i]);
 }
 
-template <int N, class T>
-static GenCoef<N, T> gen_coef(const FE1D& fe) {
-  GenCoef<N, T> P;
+template <int N, class C>
+static GenCoef<N, C> gen_coef(const FE1D& fe) {
+  GenCoef<N, C> P;
   for (int i = 0; i < N * N; ++i) {
-    P.S[i] = (T)fe.S[i];
-    P.D[i] = (T)fe.D[i];
+    P.S[i] = coef_from_double<C>(fe.S[i]);
+    P.D[i] = coef_from_double<C>(fe.D[i]);
   }
   for (int i = 0; i < N; ++i) {
-    P.d0[i] = (T)fe.dL[i];
-    P.d1[i] = (T)fe.dR[i];
+    P.d0[i] = coef_from_double<C>(fe.dL[i]);
+    P.d1[i] = coef_from_double<C>(fe.dR[i]);
   }
   return P;
 }
@@ -661,12 +664,12 @@ constexpr int gen_cpb() {
   return N <= 3 ? 16 : (N <= 5 ? 8 : (N <= 7 ? 4 : 2));
 }
 
-template <int N, class T>
+template <int N, class T, class C>
 static void gen_apply_n(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s) {
   constexpr int CPB = gen_cpb<N>(), N3 = N * N * N, N2 = N * N;
-  GenCoef<N, T> P = gen_coef<N, T>(fe);
-  size_t smem = (5 * (size_t)CPB * N3 + (size_t)CPB * 16 * N2) * sizeof(T);
-  auto kern = gen_apply_kernel<N, CPB, T>;
+  GenCoef<N, C> P = gen_coef<N, C>(fe);
+  size_t smem = (5 * (size_t)CPB * N3 + (size_t)CPB * 16 * N2) * sizeof(C);
+  auto kern = gen_apply_kernel<N, CPB, T, C>;
   static bool attr_set = false;
   if (!attr_set) {
     EXG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
@@ -674,22 +677,22 @@ static void gen_apply_n(const GeneralGeom& g, const FE1D& fe, const void* src, v
   }
   long long blocks = (g.n_cells + CPB - 1) / CPB;
   dim3 grid((unsigned)blocks, (unsigned)n_rhs);
-  kern<<<grid, CPB * N2, smem, s>>>((const T*)src, (T*)dst, P, (const T*)g.cellG, (const T*)g.face, (const T*)g.ftau,
+  kern<<<grid, CPB * N2, smem, s>>>((const T*)src, (T*)dst, P, (const C*)g.cellG, (const C*)g.face, (const C*)g.ftau,
                                     g.fnb, g.n_cells, g.n_cells * N3);
   EXG_CUDA(cudaGetLastError());
 }
 
-template <class T>
+template <class T, class C>
 static void gen_apply_t(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s) {
   switch (fe.n) {
-    case 2: gen_apply_n<2, T>(g, fe, src, dst, n_rhs, s); break;
-    case 3: gen_apply_n<3, T>(g, fe, src, dst, n_rhs, s); break;
-    case 4: gen_apply_n<4, T>(g, fe, src, dst, n_rhs, s); break;
-    case 5: gen_apply_n<5, T>(g, fe, src, dst, n_rhs, s); break;
-    case 6: gen_apply_n<6, T>(g, fe, src, dst, n_rhs, s); break;
-    case 7: gen_apply_n<7, T>(g, fe, src, dst, n_rhs, s); break;
-    case 8: gen_apply_n<8, T>(g, fe, src, dst, n_rhs, s); break;
-    case 9: gen_apply_n<9, T>(g, fe, src, dst, n_rhs, s); break;
+    case 2: gen_apply_n<2, T, C>(g, fe, src, dst, n_rhs, s); break;
+    case 3: gen_apply_n<3, T, C>(g, fe, src, dst, n_rhs, s); break;
+    case 4: gen_apply_n<4, T, C>(g, fe, src, dst, n_rhs, s); break;
+    case 5: gen_apply_n<5, T, C>(g, fe, src, dst, n_rhs, s); break;
+    case 6: gen_apply_n<6, T, C>(g, fe, src, dst, n_rhs, s); break;
+    case 7: gen_apply_n<7, T, C>(g, fe, src, dst, n_rhs, s); break;
+    case 8: gen_apply_n<8, T, C>(g, fe, src, dst, n_rhs, s); break;
+    case 9: gen_apply_n<9, T, C>(g, fe, src, dst, n_rhs, s); break;
     default: throw Error{EXG_ERR_UNSUPPORTED, "degree must be 1..8"};
   }
 }
@@ -697,9 +700,11 @@ static void gen_apply_t(const GeneralGeom& g, const FE1D& fe, const void* src, v
 void general_apply(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s) {
   EXG_CHECK(n_rhs >= 1 && n_rhs <= 65535, EXG_ERR_INVALID, "n_rhs out of range");
   if (g.precision == EXG_PREC_F32)
-    gen_apply_t<float>(g, fe, src, dst, n_rhs, s);
+    gen_apply_t<float, float>(g, fe, src, dst, n_rhs, s);
+  else if (g.precision == EXG_PREC_F64E)
+    gen_apply_t<double, df64>(g, fe, src, dst, n_rhs, s);
   else
-    gen_apply_t<double>(g, fe, src, dst, n_rhs, s);
+    gen_apply_t<double, double>(g, fe, src, dst, n_rhs, s);
 }
 
 // ------------------------------------------------------------------------------------------------
@@ -710,10 +715,10 @@ struct FETab {
   double S[100], D[100], d0[10], d1[10];
 };
 
-template <class T>
-__global__ void gen_diag_kernel(FETab F, const T* __restrict__ cellG, const T* __restrict__ face,
-                                const T* __restrict__ ftau, const long long* __restrict__ fnb, long long n_dofs,
-                                T* __restrict__ out, bool invert) {
+template <class TG, class TO>
+__global__ void gen_diag_kernel(FETab F, const TG* __restrict__ cellG, const TG* __restrict__ face,
+                                const TG* __restrict__ ftau, const long long* __restrict__ fnb, long long n_dofs,
+                                TO* __restrict__ out, bool invert) {
   const int n = F.n, n2 = n * n, n3 = n2 * n;
   long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (g >= n_dofs) return;
@@ -731,8 +736,9 @@ __global__ void gen_diag_kernel(FETab F, const T* __restrict__ cellG, const T* _
           for (int e = 0; e < 3; ++e) v *= (e == k ? F.D : F.S)[qs[e] * n + ix[e]];
           gr[k] = v;
         }
-        const T* G = cellG + (c * n3 + (q2 * n + q1) * n + q0) * 6;
-        double G00 = G[0], G01 = G[1], G02 = G[2], G11 = G[3], G12 = G[4], G22 = G[5];
+        const TG* G = cellG + (c * n3 + (q2 * n + q1) * n + q0) * 6;
+        double G00 = coef_to_double(G[0]), G01 = coef_to_double(G[1]), G02 = coef_to_double(G[2]),
+               G11 = coef_to_double(G[3]), G12 = coef_to_double(G[4]), G22 = coef_to_double(G[5]);
         sum += gr[0] * (G00 * gr[0] + G01 * gr[1] + G02 * gr[2]) + gr[1] * (G01 * gr[0] + G11 * gr[1] + G12 * gr[2]) +
                gr[2] * (G02 * gr[0] + G12 * gr[1] + G22 * gr[2]);
       }
@@ -743,18 +749,18 @@ __global__ void gen_diag_kernel(FETab F, const T* __restrict__ cellG, const T* _
     if (ix[d] != iend) continue;  // GL basis: only face nodes have a trace on the face
     long long nb = fnb[c * 6 + f];
     if (nb == -2) continue;  // Neumann
-    double tau = ftau[c * 6 + f];
+    double tau = coef_to_double(ftau[c * 6 + f]);
     const double* dside = side ? F.d1 : F.d0;
     for (int q2 = 0; q2 < n; ++q2)
       for (int q1 = 0; q1 < n; ++q1) {
-        const T* fd = face + ((c * 6 + f) * n2 + q2 * n + q1) * 7;
+        const TG* fd = face + ((c * 6 + f) * n2 + q2 * n + q1) * 7;
         double v = F.S[q1 * n + ix[t1]] * F.S[q2 * n + ix[t2]];
         double gr[3];
         gr[d] = dside[ix[d]] * F.S[q1 * n + ix[t1]] * F.S[q2 * n + ix[t2]];
         gr[t1] = F.D[q1 * n + ix[t1]] * F.S[q2 * n + ix[t2]];
         gr[t2] = F.S[q1 * n + ix[t1]] * F.D[q2 * n + ix[t2]];
-        double nd = fd[0] * gr[0] + fd[1] * gr[1] + fd[2] * gr[2];
-        double JxW = fd[6];
+        double nd = coef_to_double(fd[0]) * gr[0] + coef_to_double(fd[1]) * gr[1] + coef_to_double(fd[2]) * gr[2];
+        double JxW = coef_to_double(fd[6]);
         if (nb >= 0) {
           double s = side == 1 ? -1.0 : 1.0;
           sum += JxW * (s * v * nd + tau * v * v);
@@ -763,8 +769,8 @@ __global__ void gen_diag_kernel(FETab F, const T* __restrict__ cellG, const T* _
         }
       }
   }
-  T r = (T)sum;
-  if (invert) r = fabs((double)r) > 1e-10 ? (T)1 / r : (T)1;
+  TO r = (TO)sum;
+  if (invert) r = fabs((double)r) > 1e-10 ? (TO)1 / r : (TO)1;
   out[g] = r;
 }
 
@@ -853,11 +859,13 @@ void general_diagonal(const GeneralGeom& g, const FE1D& fe, void* out, bool inve
   long long nd = g.n_cells * fe.n * fe.n * fe.n;
   FETab F = fetab(fe);
   if (g.precision == EXG_PREC_F32)
-    gen_diag_kernel<float><<<(unsigned)((nd + 127) / 128), 128, 0, s>>>(F, (const float*)g.cellG, (const float*)g.face,
-                                                                       (const float*)g.ftau, g.fnb, nd, (float*)out,
-                                                                       invert);
+    gen_diag_kernel<float, float><<<(unsigned)((nd + 127) / 128), 128, 0, s>>>(
+        F, (const float*)g.cellG, (const float*)g.face, (const float*)g.ftau, g.fnb, nd, (float*)out, invert);
+  else if (g.precision == EXG_PREC_F64E)
+    gen_diag_kernel<df64, double><<<(unsigned)((nd + 127) / 128), 128, 0, s>>>(
+        F, (const df64*)g.cellG, (const df64*)g.face, (const df64*)g.ftau, g.fnb, nd, (double*)out, invert);
   else
-    gen_diag_kernel<double><<<(unsigned)((nd + 127) / 128), 128, 0, s>>>(
+    gen_diag_kernel<double, double><<<(unsigned)((nd + 127) / 128), 128, 0, s>>>(
         F, (const double*)g.cellG, (const double*)g.face, (const double*)g.ftau, g.fnb, nd, (double*)out, invert);
   EXG_CUDA(cudaGetLastError());
 }

@@ -60,8 +60,8 @@ def test_apply_multi_rhs(prec, k):
         assert rel(Y[r].cpu().numpy(), p.apply(X[r].astype(np.float32 if prec == E.PREC_F32 else np.float64).astype(np.float64))) <= tol
 
 
-@pytest.mark.parametrize("k", [1, 2, 3, 4, 5])
-@pytest.mark.parametrize("prec", [E.PREC_F64, E.PREC_F32])
+@pytest.mark.parametrize("k", [1, 2, 3, 4, 5, 8])
+@pytest.mark.parametrize("prec", [E.PREC_F64, E.PREC_F32, E.PREC_F64E])
 def test_apply_curved(k, prec):
     torch = require_gpu()
     p, m, op = pair("curved", 3, k, prec)
@@ -74,11 +74,12 @@ def test_apply_curved(k, prec):
     assert rel(y.cpu().numpy(), p.apply(x)) <= (1e-5 if prec == E.PREC_F32 else 1e-12)
 
 
+@pytest.mark.parametrize("prec", [E.PREC_F64, E.PREC_F64E])
 @pytest.mark.parametrize("kind", ["mixed", "periodic", "curved", "anisotropic"])
 @pytest.mark.parametrize("k", [1, 3, 5])
-def test_inverse_diagonal(kind, k):
+def test_inverse_diagonal(kind, k, prec):
     torch = require_gpu()
-    p, m, op = pair(kind, 3, k)
+    p, m, op = pair(kind, 3, k, prec)
     d = op.calculate_inverse_diagonal(op.initialize_dof_vector())
     ref = 1.0 / p.diagonal()
     assert rel(d.cpu().numpy(), ref) <= 1e-12

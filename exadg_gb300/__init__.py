@@ -70,6 +70,7 @@ class MGDesc(ctypes.Structure):
         ("min_coarse_cells", ctypes.c_int),
         ("singular", ctypes.c_int),
         ("use_graph", ctypes.c_int),
+        ("fuse_smoother", ctypes.c_int),
     ]
 
 
@@ -328,7 +329,7 @@ class MultigridPreconditioner:
 
     def __init__(self, operator, mg_precision=PREC_F32, cheb_degree=5, smoothing_range=20.0, eig_iters=20,
                  coarse_rel_tol=1e-3, coarse_abs_tol=1e-12, coarse_max_iter=10000, coarse_double=False,
-                 min_coarse_cells=2, singular=False, use_graph=True):
+                 min_coarse_cells=2, singular=False, use_graph=True, fuse_smoother=True):
         d = MGDesc()
         _check(load_library().exg_mg_default_desc(ctypes.byref(d)))
         d.mg_precision = mg_precision
@@ -342,6 +343,7 @@ class MultigridPreconditioner:
         d.min_coarse_cells = min_coarse_cells
         d.singular = int(singular)
         d.use_graph = int(use_graph)
+        d.fuse_smoother = int(fuse_smoother)
         self.desc = d
         self.operator = operator
         h = ctypes.c_void_p()

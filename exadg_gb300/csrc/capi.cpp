@@ -191,6 +191,7 @@ exg_status exg_mg_default_desc(exg_mg_desc* d) {
   d->min_coarse_cells = 2;
   d->singular = 0;
   d->use_graph = 1;
+  d->fuse_smoother = 1;
   EXG_API_END
 }
 

@@ -22,7 +22,8 @@ struct GeneralGeom {
   void build(const MeshInfo& m, const FE1D& fe, double ip, int precision, bool keep_raw, cudaStream_t s);
 };
 
-void general_apply(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s);
+void general_apply(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s,
+                   const PointEpilogue& ep = PointEpilogue());
 void general_diagonal(const GeneralGeom& g, const FE1D& fe, void* out, bool invert, cudaStream_t s);
 void general_rhs(const GeneralGeom& g, const FE1D& fe, const double* fq, const double* gq, const double* hq,
                  double* b, cudaStream_t s);

@@ -67,11 +67,11 @@ exg_op::exg_op(const MeshInfo& m, int deg, double ip_factor, int prec)
   }
 }
 
-void exg_op::apply(const void* src, void* dst, int n_rhs, cudaStream_t s) const {
+void exg_op::apply(const void* src, void* dst, int n_rhs, cudaStream_t s, const exg::PointEpilogue& ep) const {
   if (cartesian)
-    cart_apply(cart, precision, src, dst, n_rhs, cpb, s);
+    cart_apply(cart, precision, src, dst, n_rhs, cpb, s, ep);
   else
-    general_apply(*geo, fe, src, dst, n_rhs, s);
+    general_apply(*geo, fe, src, dst, n_rhs, s, ep);
 }
 
 void exg_op::diagonal(void* d, bool invert, cudaStream_t s) const {
@@ -351,6 +351,9 @@ static TransferParams make_transfer(const MGLevel& c, const MGLevel& f) {
     P.Nf[e] = f.N[e];
     P.Nc[e] = c.N[e];
   }
+  // degree pairs with a compiled transfer kernel: h at k = 1, p from k to max(k / 2, 1)
+  EXG_CHECK((P.nf == 2 && P.nc == 2) || (P.nf >= 3 && P.nf <= 9 && P.nc == (P.nf + 1) / 2), EXG_ERR_UNSUPPORTED,
+            "unsupported multigrid transfer");
   std::vector<double> zc = gauss_lobatto(P.nc), zf = gauss_lobatto(P.nf);
   if (P.is_h) {
     for (int ch = 0; ch < 2; ++ch)
@@ -451,24 +454,42 @@ void exg_mg::smooth(int l, bool zero_start, cudaStream_t s) {
       chebyshev_update<double>(mode, (double*)L.sol, (double*)L.old, (const double*)L.def, (const double*)L.tmp,
                                (const double*)L.invd, f1, f2, L.n, s);
   };
+  // fused: the operator kernel writes the new iterate into L.old, then the two buffers swap roles
+  // (the previous iterate becomes 'old' without a copy).  The swaps are host bookkeeping, so a
+  // captured graph replays the same buffer sequence every time.
+  auto step = [&](int mode, double f1, double f2) {
+    if (!desc.fuse_smoother) {
+      L.op->apply(L.sol, L.tmp, 1, s);
+      upd(mode, f1, f2);
+      return;
+    }
+    PointEpilogue ep;
+    ep.mode = mode;
+    ep.old = L.old;
+    ep.b = L.def;
+    ep.d = L.invd;
+    ep.out = L.old;
+    ep.f1 = f1;
+    ep.f2 = f2;
+    L.op->apply(L.sol, nullptr, 1, s, ep);
+    std::swap(L.sol, L.old);
+  };
   int first;
   if (zero_start) {
     upd(0, 0.0, 1.0 / L.theta);
     first = 0;
   } else {
-    L.op->apply(L.sol, L.tmp, 1, s);
-    upd(1, 0.0, 1.0 / L.theta);
+    step(1, 0.0, 1.0 / L.theta);
     first = 1;
   }
   if (deg < 2 || std::fabs(L.delta) < 1e-40) return;
   double rhok = L.delta / L.theta, sigma = L.theta / L.delta;
   for (int k = 0; k < deg - 1; ++k) {
-    L.op->apply(L.sol, L.tmp, 1, s);
     double rhokp = 1.0 / (2.0 * sigma - rhok);
     double f1 = rhokp * rhok, f2 = 2.0 * rhokp / L.delta;
     rhok = rhokp;
     int idx = k + 1 + first;
-    upd(idx == 1 ? 2 : 3, f1, f2);
+    step(idx == 1 ? 2 : 3, f1, f2);
   }
 }
 
@@ -491,14 +512,23 @@ void exg_mg::v_cycle(int l, cudaStream_t s) {
   }
   MGLevel& C = lv[l - 1];
   smooth(l, true, s);
-  L.op->apply(L.sol, L.t, 1, s);
-  if (prec == EXG_PREC_F32) {
-    rsub<float>((const float*)L.def, (float*)L.t, L.n, s);
-    restrict_add<float>(L.tr, (const float*)L.t, (float*)C.def, s);
+  if (desc.fuse_smoother) {  // t = def - A sol in the operator's store
+    PointEpilogue ep;
+    ep.mode = 4;
+    ep.b = L.def;
+    ep.out = L.t;
+    L.op->apply(L.sol, nullptr, 1, s, ep);
   } else {
-    rsub<double>((const double*)L.def, (double*)L.t, L.n, s);
-    restrict_add<double>(L.tr, (const double*)L.t, (double*)C.def, s);
+    L.op->apply(L.sol, L.t, 1, s);
+    if (prec == EXG_PREC_F32)
+      rsub<float>((const float*)L.def, (float*)L.t, L.n, s);
+    else
+      rsub<double>((const double*)L.def, (double*)L.t, L.n, s);
   }
+  if (prec == EXG_PREC_F32)
+    restrict_add<float>(L.tr, (const float*)L.t, (float*)C.def, s);
+  else
+    restrict_add<double>(L.tr, (const double*)L.t, (double*)C.def, s);
   v_cycle(l - 1, s);
   if (prec == EXG_PREC_F32)
     prolongate_add<float>(L.tr, (const float*)C.sol, (float*)L.sol, s);

@@ -42,7 +42,8 @@ struct exg_op {
 
   exg_op(const exg::MeshInfo& m, int degree, double ip, int precision);
   long long n_dofs() const { return mesh.n_cells() * n * n * n; }
-  void apply(const void* src, void* dst, int n_rhs, cudaStream_t s) const;
+  void apply(const void* src, void* dst, int n_rhs, cudaStream_t s,
+             const exg::PointEpilogue& ep = exg::PointEpilogue()) const;
   void diagonal(void* d, bool invert, cudaStream_t s) const;
   void quadrature_points(double* cx, double* fx, long long* ncp, long long* nfp, cudaStream_t s);
   void rhs(const double* f, const double* g, const double* h, double* b, cudaStream_t s);

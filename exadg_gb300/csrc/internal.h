@@ -89,9 +89,26 @@ struct CartHost {
 };
 void build_cart_host(const MeshInfo& m, const FE1D& fe, double ip, CartHost& out);
 
+// Point-wise update fused into the operator's store: with t = (A x)_i for the DoF i the kernel
+// writes out_i instead of t (vectors in the operator's storage type, one right-hand side):
+//   mode -1: out = dst, out_i = t                           (plain apply)
+//   mode  1: out_i = x_i + f2 d_i (b_i - t)                 (Chebyshev step, first update)
+//   mode  2: out_i = (1 + f1) x_i + f2 d_i (b_i - t)        (second update after a zero start)
+//   mode  3: out_i = (1 + f1) x_i - f1 old_i + f2 d_i (b_i - t)
+//   mode  4: out_i = b_i - t                                (residual)
+// out may alias old (each index is read and then written by the same thread); it must not alias x.
+struct PointEpilogue {
+  int mode = -1;
+  const void* old = nullptr;
+  const void* b = nullptr;
+  const void* d = nullptr;
+  void* out = nullptr;
+  double f1 = 0, f2 = 0;
+};
+
 // precision: EXG_PREC_F64 / EXG_PREC_F32 / EXG_PREC_F64E; cpb = cells per block (0 = default)
 void cart_apply(const CartHost& h, int precision, const void* src, void* dst, int n_rhs, int cpb,
-                cudaStream_t s);
+                cudaStream_t s, const PointEpilogue& ep = PointEpilogue());
 void cart_diagonal(const CartHost& h, int precision, void* diag, bool invert, cudaStream_t s);
 std::vector<int> cart_cpb_options(int n, int precision);
 

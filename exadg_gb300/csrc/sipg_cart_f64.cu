@@ -3,7 +3,8 @@
 #include "sipg_cartesian.cuh"
 
 namespace exg {
-void cart_apply_f64(const CartHost& h, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s) {
-  apply_prec<double, double>(h, src, dst, n_rhs, cpb, s);
+void cart_apply_f64(const CartHost& h, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s,
+                     const PointEpilogue& ep) {
+  apply_prec<double, double>(h, src, dst, n_rhs, cpb, s, ep);
 }
 }  // namespace exg

@@ -4,17 +4,22 @@
 
 namespace exg {
 
-void cart_apply_f64(const CartHost& h, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s);
-void cart_apply_f32(const CartHost& h, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s);
-void cart_apply_df64(const CartHost& h, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s);
+void cart_apply_f64(const CartHost& h, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s,
+                    const PointEpilogue& ep);
+void cart_apply_f32(const CartHost& h, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s,
+                    const PointEpilogue& ep);
+void cart_apply_df64(const CartHost& h, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s,
+                    const PointEpilogue& ep);
 
-void cart_apply(const CartHost& h, int precision, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s) {
+void cart_apply(const CartHost& h, int precision, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s,
+                const PointEpilogue& ep) {
+  EXG_CHECK(ep.mode < 0 || n_rhs == 1, EXG_ERR_INVALID, "fused point update needs a single right-hand side");
   if (precision == EXG_PREC_F64)
-    cart_apply_f64(h, src, dst, n_rhs, cpb, s);
+    cart_apply_f64(h, src, dst, n_rhs, cpb, s, ep);
   else if (precision == EXG_PREC_F32)
-    cart_apply_f32(h, src, dst, n_rhs, cpb, s);
+    cart_apply_f32(h, src, dst, n_rhs, cpb, s, ep);
   else if (precision == EXG_PREC_F64E)
-    cart_apply_df64(h, src, dst, n_rhs, cpb, s);
+    cart_apply_df64(h, src, dst, n_rhs, cpb, s, ep);
   else
     throw Error{EXG_ERR_INVALID, "unknown precision"};
 }

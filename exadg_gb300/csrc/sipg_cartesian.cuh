@@ -22,6 +22,7 @@
 #include <stdexcept>
 
 #include "df64.cuh"
+#include "epilogue.cuh"
 #include "internal.h"
 
 namespace exg {
@@ -276,7 +277,7 @@ __device__ __forceinline__ void mass_line(C* __restrict__ x, int a, int b, const
 template <int N, int CPB, class T, class C>
 __global__ void __launch_bounds__(CPB* N* N) cart_apply_kernel(const T* __restrict__ src, T* __restrict__ dst,
                                                                const __grid_constant__ CartCoef<N, C> P,
-                                                               const CartMesh m) {
+                                                               const CartMesh m, const PointEpilogue ep) {
   constexpr int N2 = N * N, N3 = N2 * N, NT = CPB * N2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* stau = reinterpret_cast<C*>(smem_raw);             // CPB*6
@@ -336,13 +337,12 @@ __global__ void __launch_bounds__(CPB* N* N) cart_apply_kernel(const T* __restri
       int id = line_index<2, N>(k, a, b);
       v[k] = wx[co + id] + wy[co + id];
     }
-    T* oc = o + base + co;
     C r[N];
     eo_matvec<N, C>(P.M, P.Me, P.Mo, P.Mm, v, r);
 #pragma unroll
     for (int k = 0; k < N; ++k) {
       int id = line_index<2, N>(k, a, b);
-      store_as<T>(oc + id, r[k] + wz[co + id]);
+      epilogue_store<T>(ep, o, base + co + id, s, to_storage<T>(r[k] + wz[co + id]));
     }
   }
 }
@@ -436,7 +436,7 @@ __host__ __device__ constexpr size_t brick_head_bytes(int nown, int nslot) {
 template <int N, int BX, int BY, int BZ, class T, class C>
 __global__ void __launch_bounds__(BX* BY* BZ* N* N)
     cart_brick_kernel(const T* __restrict__ src, T* __restrict__ dst, const __grid_constant__ CartCoef<N, C> P,
-                      const CartMesh m, int nbx, int nby) {
+                      const CartMesh m, int nbx, int nby, const PointEpilogue ep) {
   using B = Brick<BX, BY, BZ>;
   constexpr int N2 = N * N, N3 = N2 * N, NT = B::NOWN * N2;
   static_assert(NT >= 32, "brick needs at least one full warp");
@@ -584,13 +584,12 @@ __global__ void __launch_bounds__(BX* BY* BZ* N* N)
       v[k] = wx[co + id] + wy[co + id];
     }
     const long long gc = (long long)(x0[0] + lx) + (long long)m.N[0] * ((x0[1] + ly) + (long long)m.N[1] * (x0[2] + lz));
-    T* oc = o + gc * N3;
     C r[N];
     eo_matvec<N, C>(P.M, P.Me, P.Mo, P.Mm, v, r);
 #pragma unroll
     for (int k = 0; k < N; ++k) {
       int id = line_index<2, N>(k, a, b);
-      store_as<T>(oc + id, r[k] + wz[co + id]);
+      epilogue_store<T>(ep, o, gc * N3 + id, s, to_storage<T>(r[k] + wz[co + id]));
     }
   }
 }
@@ -650,7 +649,8 @@ template <> struct CpbChoice<8> { static constexpr int a = 1, b = 2, c = 4; };
 template <> struct CpbChoice<9> { static constexpr int a = 1, b = 2, c = 4; };
 
 template <int N, int CPB, class T, class C>
-static void launch_apply(const CartHost& h, const void* src, void* dst, int n_rhs, cudaStream_t s) {
+static void launch_apply(const CartHost& h, const void* src, void* dst, int n_rhs, cudaStream_t s,
+                         const PointEpilogue& ep) {
   constexpr int N3 = N * N * N;
   CartCoef<N, C> P = make_coef<N, C>(h);
   size_t smem = smem_head_bytes<C>(CPB) + 4 * (size_t)CPB * N3 * sizeof(C);
@@ -664,12 +664,13 @@ static void launch_apply(const CartHost& h, const void* src, void* dst, int n_rh
   EXG_CHECK(blocks < (1LL << 31), EXG_ERR_INVALID, "mesh too large");
   EXG_CHECK(n_rhs >= 1 && n_rhs <= 65535, EXG_ERR_INVALID, "n_rhs out of range");
   dim3 grid((unsigned)blocks, (unsigned)n_rhs);
-  kern<<<grid, CPB * N * N, smem, s>>>((const T*)src, (T*)dst, P, h.mesh);
+  kern<<<grid, CPB * N * N, smem, s>>>((const T*)src, (T*)dst, P, h.mesh, ep);
   EXG_CUDA(cudaGetLastError());
 }
 
 template <int N, int BX, int BY, int BZ, class T, class C>
-static void launch_brick(const CartHost& h, const void* src, void* dst, int n_rhs, cudaStream_t s) {
+static void launch_brick(const CartHost& h, const void* src, void* dst, int n_rhs, cudaStream_t s,
+                         const PointEpilogue& ep) {
   using Bk = Brick<BX, BY, BZ>;
   constexpr int N3 = N * N * N;
   CartCoef<N, C> P = make_coef<N, C>(h);
@@ -686,7 +687,7 @@ static void launch_brick(const CartHost& h, const void* src, void* dst, int n_rh
   EXG_CHECK(blocks < (1LL << 31), EXG_ERR_INVALID, "mesh too large");
   EXG_CHECK(n_rhs >= 1 && n_rhs <= 65535, EXG_ERR_INVALID, "n_rhs out of range");
   dim3 grid((unsigned)blocks, (unsigned)n_rhs);
-  kern<<<grid, Bk::NOWN * N * N, smem, s>>>((const T*)src, (T*)dst, P, h.mesh, nb[0], nb[1]);
+  kern<<<grid, Bk::NOWN * N * N, smem, s>>>((const T*)src, (T*)dst, P, h.mesh, nb[0], nb[1], ep);
   EXG_CUDA(cudaGetLastError());
 }
 
@@ -702,31 +703,33 @@ template <> struct BrickChoice<8> { static constexpr int ax = 2, ay = 1, az = 1,
 template <> struct BrickChoice<9> { static constexpr int ax = 1, ay = 1, az = 1, bx = 2, by = 1, bz = 1; };
 
 template <int N, class T, class C>
-static void apply_n(const CartHost& h, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s) {
+static void apply_n(const CartHost& h, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s,
+                    const PointEpilogue& ep) {
   using BC = BrickChoice<N>;
   if (cpb == -1)
-    launch_brick<N, BC::ax, BC::ay, BC::az, T, C>(h, src, dst, n_rhs, s);
+    launch_brick<N, BC::ax, BC::ay, BC::az, T, C>(h, src, dst, n_rhs, s, ep);
   else if (cpb == -2)
-    launch_brick<N, BC::bx, BC::by, BC::bz, T, C>(h, src, dst, n_rhs, s);
+    launch_brick<N, BC::bx, BC::by, BC::bz, T, C>(h, src, dst, n_rhs, s, ep);
   else if (cpb == CpbChoice<N>::a)
-    launch_apply<N, CpbChoice<N>::a, T, C>(h, src, dst, n_rhs, s);
+    launch_apply<N, CpbChoice<N>::a, T, C>(h, src, dst, n_rhs, s, ep);
   else if (cpb == CpbChoice<N>::c)
-    launch_apply<N, CpbChoice<N>::c, T, C>(h, src, dst, n_rhs, s);
+    launch_apply<N, CpbChoice<N>::c, T, C>(h, src, dst, n_rhs, s, ep);
   else
-    launch_apply<N, CpbChoice<N>::b, T, C>(h, src, dst, n_rhs, s);
+    launch_apply<N, CpbChoice<N>::b, T, C>(h, src, dst, n_rhs, s, ep);
 }
 
 template <class T, class C>
-static void apply_prec(const CartHost& h, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s) {
+static void apply_prec(const CartHost& h, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s,
+                       const PointEpilogue& ep) {
   switch (h.n) {
-    case 2: apply_n<2, T, C>(h, src, dst, n_rhs, cpb, s); break;
-    case 3: apply_n<3, T, C>(h, src, dst, n_rhs, cpb, s); break;
-    case 4: apply_n<4, T, C>(h, src, dst, n_rhs, cpb, s); break;
-    case 5: apply_n<5, T, C>(h, src, dst, n_rhs, cpb, s); break;
-    case 6: apply_n<6, T, C>(h, src, dst, n_rhs, cpb, s); break;
-    case 7: apply_n<7, T, C>(h, src, dst, n_rhs, cpb, s); break;
-    case 8: apply_n<8, T, C>(h, src, dst, n_rhs, cpb, s); break;
-    case 9: apply_n<9, T, C>(h, src, dst, n_rhs, cpb, s); break;
+    case 2: apply_n<2, T, C>(h, src, dst, n_rhs, cpb, s, ep); break;
+    case 3: apply_n<3, T, C>(h, src, dst, n_rhs, cpb, s, ep); break;
+    case 4: apply_n<4, T, C>(h, src, dst, n_rhs, cpb, s, ep); break;
+    case 5: apply_n<5, T, C>(h, src, dst, n_rhs, cpb, s, ep); break;
+    case 6: apply_n<6, T, C>(h, src, dst, n_rhs, cpb, s, ep); break;
+    case 7: apply_n<7, T, C>(h, src, dst, n_rhs, cpb, s, ep); break;
+    case 8: apply_n<8, T, C>(h, src, dst, n_rhs, cpb, s, ep); break;
+    case 9: apply_n<9, T, C>(h, src, dst, n_rhs, cpb, s, ep); break;
     default: throw Error{EXG_ERR_UNSUPPORTED, "degree must be 1..8"};
   }
 }

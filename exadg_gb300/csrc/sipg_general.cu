@@ -16,6 +16,7 @@
 #include <cmath>
 
 #include "df64.cuh"
+#include "epilogue.cuh"
 #include "general.h"
 #include "internal.h"
 
@@ -346,7 +347,7 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
                                                               const C* __restrict__ cellG, const C* __restrict__ face,
                                                               const C* __restrict__ ftau,
                                                               const long long* __restrict__ fnb, long long n_cells,
-                                                              long long n_dofs) {
+                                                              long long n_dofs, const PointEpilogue ep) {
   constexpr int N2 = N * N, N3 = N2 * N, NT = CPB * N2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* su = reinterpret_cast<C*>(smem_raw);
@@ -355,6 +356,14 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
   C* t1 = t0 + CPB * N3;
   C* t2 = t1 + CPB * N3;
   C* fsh = t2 + CPB * N3;  // CPB * 16 * N2 face scratch
+
+  // 1D matrices for the face stages, where the row index differs between the threads of a warp:
+  // read from shared memory (a kernel-parameter read with a per-thread index is serialised)
+  __shared__ C sS[N2], sD[N2];
+  for (int i = threadIdx.x; i < N2; i += NT) {
+    sS[i] = P.S[i];
+    sD[i] = P.D[i];
+  }
 
   const long long c0 = (long long)blockIdx.x * CPB;
   const T* s = src + (long long)blockIdx.y * n_dofs;
@@ -541,7 +550,7 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
     if (active && nb != -2) {
       C sv = C(0), sdv = C(0), sn = 0, nv = C(0), ndv = 0, nn = C(0);
       for (int k = 0; k < N; ++k) {
-        C Sq = P.S[p1 * N + k], Dq = P.D[p1 * N + k];
+        C Sq = sS[p1 * N + k], Dq = sD[p1 * N + k];
         sv = fmadd(Sq, fv[p2 * N + k], sv);
         sdv = fmadd(Dq, fv[p2 * N + k], sdv);
         sn = fmadd(Sq, fn[p2 * N + k], sn);
@@ -564,7 +573,7 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
     if (active && nb != -2) {
       C vo = C(0), go_t1 = C(0), go_t2 = 0, go_d = C(0), vn = 0, gn_t1 = C(0), gn_t2 = 0, gn_d = C(0);
       for (int k = 0; k < N; ++k) {
-        C Sq = P.S[p2 * N + k], Dq = P.D[p2 * N + k];
+        C Sq = sS[p2 * N + k], Dq = sD[p2 * N + k];
         vo = fmadd(Sq, r0[k * N + p1], vo);
         go_t2 = fmadd(Dq, r0[k * N + p1], go_t2);
         go_t1 = fmadd(Sq, r1[k * N + p1], go_t1);
@@ -615,7 +624,7 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
     if (active && nb != -2) {
       C s1 = C(0), s2 = C(0), s3 = 0, s4 = C(0);
       for (int q = 0; q < N; ++q) {
-        C Sq = P.S[q * N + p2], Dq = P.D[q * N + p2];
+        C Sq = sS[q * N + p2], Dq = sD[q * N + p2];
         s1 = fmadd(Sq, cv[q * N + p1], s1);
         s2 = fmadd(Sq, c1_[q * N + p1], s2);
         s3 = fmadd(Dq, c2_[q * N + p1], s3);
@@ -631,7 +640,7 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
     if (active && nb != -2) {
       C tv = C(0), tn = C(0);
       for (int q = 0; q < N; ++q) {
-        C Sq = P.S[q * N + p1], Dq = P.D[q * N + p1];
+        C Sq = sS[q * N + p1], Dq = sD[q * N + p1];
         tv = fmadd(Sq, r0[p2 * N + q], tv);
         tv = fmadd(Dq, r1[p2 * N + q], tv);
         tv = fmadd(Sq, r2[p2 * N + q], tv);
@@ -642,7 +651,7 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
     }
     __syncthreads();
   }
-  for (int i = tid; i < nd; i += NT) store_as<T>(o + base + i, so[i]);
+  for (int i = tid; i < nd; i += NT) epilogue_store<T>(ep, o, base + i, s, to_storage<T>(so[i]));
 }
 
 template <int N, class C>
@@ -665,7 +674,8 @@ constexpr int gen_cpb() {
 }
 
 template <int N, class T, class C>
-static void gen_apply_n(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s) {
+static void gen_apply_n(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s,
+                        const PointEpilogue& ep) {
   constexpr int CPB = gen_cpb<N>(), N3 = N * N * N, N2 = N * N;
   GenCoef<N, C> P = gen_coef<N, C>(fe);
   size_t smem = (5 * (size_t)CPB * N3 + (size_t)CPB * 16 * N2) * sizeof(C);
@@ -678,33 +688,36 @@ static void gen_apply_n(const GeneralGeom& g, const FE1D& fe, const void* src, v
   long long blocks = (g.n_cells + CPB - 1) / CPB;
   dim3 grid((unsigned)blocks, (unsigned)n_rhs);
   kern<<<grid, CPB * N2, smem, s>>>((const T*)src, (T*)dst, P, (const C*)g.cellG, (const C*)g.face, (const C*)g.ftau,
-                                    g.fnb, g.n_cells, g.n_cells * N3);
+                                    g.fnb, g.n_cells, g.n_cells * N3, ep);
   EXG_CUDA(cudaGetLastError());
 }
 
 template <class T, class C>
-static void gen_apply_t(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s) {
+static void gen_apply_t(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s,
+                        const PointEpilogue& ep) {
   switch (fe.n) {
-    case 2: gen_apply_n<2, T, C>(g, fe, src, dst, n_rhs, s); break;
-    case 3: gen_apply_n<3, T, C>(g, fe, src, dst, n_rhs, s); break;
-    case 4: gen_apply_n<4, T, C>(g, fe, src, dst, n_rhs, s); break;
-    case 5: gen_apply_n<5, T, C>(g, fe, src, dst, n_rhs, s); break;
-    case 6: gen_apply_n<6, T, C>(g, fe, src, dst, n_rhs, s); break;
-    case 7: gen_apply_n<7, T, C>(g, fe, src, dst, n_rhs, s); break;
-    case 8: gen_apply_n<8, T, C>(g, fe, src, dst, n_rhs, s); break;
-    case 9: gen_apply_n<9, T, C>(g, fe, src, dst, n_rhs, s); break;
+    case 2: gen_apply_n<2, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
+    case 3: gen_apply_n<3, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
+    case 4: gen_apply_n<4, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
+    case 5: gen_apply_n<5, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
+    case 6: gen_apply_n<6, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
+    case 7: gen_apply_n<7, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
+    case 8: gen_apply_n<8, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
+    case 9: gen_apply_n<9, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
     default: throw Error{EXG_ERR_UNSUPPORTED, "degree must be 1..8"};
   }
 }
 
-void general_apply(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s) {
+void general_apply(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s,
+                   const PointEpilogue& ep) {
   EXG_CHECK(n_rhs >= 1 && n_rhs <= 65535, EXG_ERR_INVALID, "n_rhs out of range");
+  EXG_CHECK(ep.mode < 0 || n_rhs == 1, EXG_ERR_INVALID, "fused point update needs a single right-hand side");
   if (g.precision == EXG_PREC_F32)
-    gen_apply_t<float, float>(g, fe, src, dst, n_rhs, s);
+    gen_apply_t<float, float>(g, fe, src, dst, n_rhs, s, ep);
   else if (g.precision == EXG_PREC_F64E)
-    gen_apply_t<double, df64>(g, fe, src, dst, n_rhs, s);
+    gen_apply_t<double, df64>(g, fe, src, dst, n_rhs, s, ep);
   else
-    gen_apply_t<double, double>(g, fe, src, dst, n_rhs, s);
+    gen_apply_t<double, double>(g, fe, src, dst, n_rhs, s, ep);
 }
 
 // ------------------------------------------------------------------------------------------------

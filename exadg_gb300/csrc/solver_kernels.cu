@@ -5,6 +5,9 @@
 // adds the partials in index order (no floating-point atomics).
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
+#include "epilogue.cuh"
 #include "internal.h"
 #include "solver_kernels.h"
 
@@ -173,14 +176,7 @@ __global__ void cheb_kernel(int mode, T* __restrict__ x, T* __restrict__ old, co
       continue;
     }
     T xi = x[i];
-    T pr = d[i] * (b[i] - t[i]);
-    T xn;
-    if (mode == 1)
-      xn = xi + f2 * pr;
-    else if (mode == 2)
-      xn = (T(1) + f1) * xi + f2 * pr;
-    else
-      xn = (T(1) + f1) * xi - f1 * old[i] + f2 * pr;
+    T xn = cheb_point<T>(mode, xi, mode == 3 ? old[i] : T(0), b[i], t[i], d[i], f1, f2);
     old[i] = xi;
     x[i] = xn;
   }
@@ -210,106 +206,239 @@ void rsub(const T* b, T* t, long long n, cudaStream_t s) {
 }
 
 // ------------------------------------------------------------------------------------------------
-// DG transfers (MGTwoLevelTransfer, element-local interpolation; restriction = transpose)
+// DG transfers (MGTwoLevelTransfer, element-local interpolation; restriction = transpose), sum
+// factorised: per fine cell the 3D interpolation P2 x P1 x P0 is applied as three 1D sweeps through
+// shared memory (nf nc^3 + nf^2 nc^2 + nf^3 nc multiply-adds instead of nf^3 nc^3), in the
+// multigrid's own number type.  A block handles G consecutive cells; for h-transfers the 1D matrix
+// of each direction is the one of the cell's child position in its parent.
 // ------------------------------------------------------------------------------------------------
-template <class T>
-__global__ void prolongate_kernel(TransferParams P, const T* __restrict__ coarse, T* __restrict__ fine, long long n_fine) {
-  long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= n_fine) return;
-  const int nf = P.nf, nc = P.nc, nf3 = nf * nf * nf, nc3 = nc * nc * nc;
-  long long cf = g / nf3;
-  int loc = (int)(g - cf * nf3);
-  int ix[3] = {loc % nf, (loc / nf) % nf, loc / (nf * nf)};
-  int ci[3] = {(int)(cf % P.Nf[0]), (int)((cf / P.Nf[0]) % P.Nf[1]), (int)(cf / ((long long)P.Nf[0] * P.Nf[1]))};
-  int ch[3] = {0, 0, 0};
-  long long cc = cf;
-  if (P.is_h) {
-    for (int e = 0; e < 3; ++e) ch[e] = ci[e] & 1;
-    cc = (ci[0] >> 1) + (long long)P.Nc[0] * ((ci[1] >> 1) + (long long)P.Nc[1] * (ci[2] >> 1));
-  }
-  const T* u = coarse + cc * nc3;
-  const double* P0 = P.P[ch[0]] + ix[0] * nc;
-  const double* P1 = P.P[ch[1]] + ix[1] * nc;
-  const double* P2 = P.P[ch[2]] + ix[2] * nc;
-  double s = 0;
-  for (int c2 = 0; c2 < nc; ++c2)
-    for (int c1 = 0; c1 < nc; ++c1) {
-      double w = P2[c2] * P1[c1];
-      const T* ul = u + (c2 * nc + c1) * nc;
-      for (int c0 = 0; c0 < nc; ++c0) s += w * P0[c0] * (double)ul[c0];
+template <int NF>
+struct TransferShape {
+  static constexpr int G = 512 / (NF * NF * NF) < 1 ? 1 : 512 / (NF * NF * NF);  // cells per block
+};
+
+template <int NF, int NC, class T>
+__global__ void __launch_bounds__(256) prolongate_kernel(const __grid_constant__ TransferParams P,
+                                                         const T* __restrict__ coarse, T* __restrict__ fine,
+                                                         long long n_cells) {
+  constexpr int nf = NF, nc = NC, nf2 = nf * nf, nf3 = nf2 * nf, nc2 = nc * nc, nc3 = nc2 * nc;
+  constexpr int G = TransferShape<NF>::G;
+  __shared__ T Ps[2 * nf * nc];  // [child][nf][nc]
+  __shared__ T u[G * nc3];       // [G][nc3]
+  __shared__ T t1[G * nc2 * nf];  // [G][c2][c1][i0]
+  __shared__ T t2[G * nc * nf2];  // [G][c2][i1][i0]
+  __shared__ int chs[G];          // child position bits per cell
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const long long cell0 = (long long)blockIdx.x * G;
+  const int ncell = (int)min((long long)G, n_cells - cell0);
+  for (int e = tid; e < 2 * nf * nc; e += nt) Ps[e] = (T)P.P[e / (nf * nc)][e % (nf * nc)];
+  for (int lc = tid; lc < ncell; lc += nt) {
+    long long cf = cell0 + lc;
+    int code = 0;
+    if (P.is_h) {
+      int cx = (int)(cf % P.Nf[0]), cy = (int)((cf / P.Nf[0]) % P.Nf[1]),
+          cz = (int)(cf / ((long long)P.Nf[0] * P.Nf[1]));
+      code = (cx & 1) | ((cy & 1) << 1) | ((cz & 1) << 2);
     }
-  fine[g] += (T)s;
+    chs[lc] = code;
+  }
+  for (int e = tid; e < ncell * nc3; e += nt) {
+    int lc = e / nc3, j = e - lc * nc3;
+    long long cf = cell0 + lc, cc = cf;
+    if (P.is_h) {
+      int cx = (int)(cf % P.Nf[0]), cy = (int)((cf / P.Nf[0]) % P.Nf[1]),
+          cz = (int)(cf / ((long long)P.Nf[0] * P.Nf[1]));
+      cc = (cx >> 1) + (long long)P.Nc[0] * ((cy >> 1) + (long long)P.Nc[1] * (cz >> 1));
+    }
+    u[e] = coarse[cc * nc3 + j];
+  }
+  __syncthreads();
+  for (int e = tid; e < ncell * nc2 * nf; e += nt) {  // x
+    int lc = e / (nc2 * nf), r = e - lc * nc2 * nf, i0 = r % nf, c21 = r / nf;
+    const T* Pm = Ps + (chs[lc] & 1) * nf * nc + i0 * nc;
+    const T* ul = u + lc * nc3 + c21 * nc;
+    T acc = 0;
+#pragma unroll
+    for (int c = 0; c < nc; ++c) acc += Pm[c] * ul[c];
+    t1[e] = acc;
+  }
+  __syncthreads();
+  for (int e = tid; e < ncell * nc * nf2; e += nt) {  // y
+    int lc = e / (nc * nf2), r = e - lc * nc * nf2, i0 = r % nf, i1 = (r / nf) % nf, c2 = r / nf2;
+    const T* Pm = Ps + ((chs[lc] >> 1) & 1) * nf * nc + i1 * nc;
+    const T* tl = t1 + lc * nc2 * nf + c2 * nc * nf + i0;
+    T acc = 0;
+#pragma unroll
+    for (int c = 0; c < nc; ++c) acc += Pm[c] * tl[c * nf];
+    t2[e] = acc;
+  }
+  __syncthreads();
+  for (int e = tid; e < ncell * nf3; e += nt) {  // z, accumulate into the fine vector
+    int lc = e / nf3, r = e - lc * nf3, i01 = r % nf2, i2 = r / nf2;
+    const T* Pm = Ps + ((chs[lc] >> 2) & 1) * nf * nc + i2 * nc;
+    const T* tl = t2 + lc * nc * nf2 + i01;
+    T acc = 0;
+#pragma unroll
+    for (int c = 0; c < nc; ++c) acc += Pm[c] * tl[c * nf2];
+    fine[cell0 * nf3 + e] += acc;
+  }
 }
 
-template <class T>
-__global__ void restrict_kernel(TransferParams P, const T* __restrict__ fine, T* __restrict__ coarse, long long n_coarse) {
-  long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (g >= n_coarse) return;
-  const int nf = P.nf, nc = P.nc, nf3 = nf * nf * nf, nc3 = nc * nc * nc;
-  long long cc = g / nc3;
-  int loc = (int)(g - cc * nc3);
-  int jx[3] = {loc % nc, (loc / nc) % nc, loc / (nc * nc)};
-  int ci[3] = {(int)(cc % P.Nc[0]), (int)((cc / P.Nc[0]) % P.Nc[1]), (int)(cc / ((long long)P.Nc[0] * P.Nc[1]))};
-  double s = 0;
-  int nch = P.is_h ? 8 : 1;
+template <int NF, int NC, class T>
+__global__ void __launch_bounds__(256) restrict_kernel(const __grid_constant__ TransferParams P,
+                                                       const T* __restrict__ fine, T* __restrict__ coarse,
+                                                       long long n_cells) {
+  constexpr int nf = NF, nc = NC, nf2 = nf * nf, nf3 = nf2 * nf, nc2 = nc * nc, nc3 = nc2 * nc;
+  constexpr int G = TransferShape<NF>::G;
+  __shared__ T Ps[2 * nf * nc];    // [child][nf][nc]
+  __shared__ T f[G * nf3];         // [G][nf3]
+  __shared__ T t1[G * nf2 * nc];   // [G][i2][i1][j0]
+  __shared__ T t2[G * nf * nc2];   // [G][i2][j1][j0]
+  __shared__ T acc[G * nc3];       // [G][nc3]
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const long long cell0 = (long long)blockIdx.x * G;
+  const int ncell = (int)min((long long)G, n_cells - cell0);
+  for (int e = tid; e < 2 * nf * nc; e += nt) Ps[e] = (T)P.P[e / (nf * nc)][e % (nf * nc)];
+  for (int e = tid; e < ncell * nc3; e += nt) acc[e] = 0;
+  const int nch = P.is_h ? 8 : 1;
   for (int c8 = 0; c8 < nch; ++c8) {
-    int ch[3] = {c8 & 1, (c8 >> 1) & 1, (c8 >> 2) & 1};
-    long long cf = cc;
-    if (P.is_h)
-      cf = (2 * ci[0] + ch[0]) + (long long)P.Nf[0] * ((2 * ci[1] + ch[1]) + (long long)P.Nf[1] * (2 * ci[2] + ch[2]));
-    else
-      ch[0] = ch[1] = ch[2] = 0;
-    const T* u = fine + cf * nf3;
-    for (int i2 = 0; i2 < nf; ++i2)
-      for (int i1 = 0; i1 < nf; ++i1) {
-        double w = P.P[ch[2]][i2 * nc + jx[2]] * P.P[ch[1]][i1 * nc + jx[1]];
-        const T* ul = u + (i2 * nf + i1) * nf;
-        for (int i0 = 0; i0 < nf; ++i0) s += w * P.P[ch[0]][i0 * nc + jx[0]] * (double)ul[i0];
+    const int ch0 = c8 & 1, ch1 = (c8 >> 1) & 1, ch2 = (c8 >> 2) & 1;
+    for (int e = tid; e < ncell * nf3; e += nt) {
+      int lc = e / nf3, i = e - lc * nf3;
+      long long cc = cell0 + lc, cf = cc;
+      if (P.is_h) {
+        int cx = (int)(cc % P.Nc[0]), cy = (int)((cc / P.Nc[0]) % P.Nc[1]),
+            cz = (int)(cc / ((long long)P.Nc[0] * P.Nc[1]));
+        cf = (2 * cx + ch0) + (long long)P.Nf[0] * ((2 * cy + ch1) + (long long)P.Nf[1] * (2 * cz + ch2));
       }
+      f[e] = fine[cf * nf3 + i];
+    }
+    __syncthreads();
+    const T* P0 = Ps + (P.is_h ? ch0 : 0) * nf * nc;
+    const T* P1 = Ps + (P.is_h ? ch1 : 0) * nf * nc;
+    const T* P2 = Ps + (P.is_h ? ch2 : 0) * nf * nc;
+    for (int e = tid; e < ncell * nf2 * nc; e += nt) {  // x^T
+      int lc = e / (nf2 * nc), r = e - lc * nf2 * nc, j0 = r % nc, i21 = r / nc;
+      const T* fl = f + lc * nf3 + i21 * nf;
+      T a = 0;
+#pragma unroll
+      for (int i = 0; i < nf; ++i) a += P0[i * nc + j0] * fl[i];
+      t1[e] = a;
+    }
+    __syncthreads();
+    for (int e = tid; e < ncell * nf * nc2; e += nt) {  // y^T
+      int lc = e / (nf * nc2), r = e - lc * nf * nc2, j0 = r % nc, j1 = (r / nc) % nc, i2 = r / nc2;
+      const T* tl = t1 + lc * nf2 * nc + i2 * nf * nc + j0;
+      T a = 0;
+#pragma unroll
+      for (int i = 0; i < nf; ++i) a += P1[i * nc + j1] * tl[i * nc];
+      t2[e] = a;
+    }
+    __syncthreads();
+    for (int e = tid; e < ncell * nc3; e += nt) {  // z^T, accumulated over the children
+      int lc = e / nc3, r = e - lc * nc3, j01 = r % nc2, j2 = r / nc2;
+      const T* tl = t2 + lc * nf * nc2 + j01;
+      T a = 0;
+#pragma unroll
+      for (int i = 0; i < nf; ++i) a += P2[i * nc + j2] * tl[i * nc2];
+      acc[e] += a;
+    }
+    __syncthreads();
   }
-  coarse[g] += (T)s;
+  for (int e = tid; e < ncell * nc3; e += nt) coarse[cell0 * nc3 + e] += acc[e];
 }
+
+// (nf, nc) pairs of the level sequence: h-transfers at k = 1 and the Bisect p-sequence k -> k/2
+#define EXG_TRANSFER_PAIRS(X) X(2, 2) X(3, 2) X(4, 2) X(5, 3) X(6, 3) X(7, 4) X(8, 4) X(9, 5)
 
 template <class T>
 void prolongate_add(const TransferParams& P, const T* coarse, T* fine, cudaStream_t s) {
-  long long n = (long long)P.Nf[0] * P.Nf[1] * P.Nf[2] * P.nf * P.nf * P.nf;
-  prolongate_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P, coarse, fine, n);
-  EXG_CUDA(cudaGetLastError());
+  long long cells = (long long)P.Nf[0] * P.Nf[1] * P.Nf[2];
+#define EXG_PROLONG(NF, NC)                                                                        \
+  if (P.nf == NF && P.nc == NC) {                                                                  \
+    constexpr int G = TransferShape<NF>::G;                                                        \
+    prolongate_kernel<NF, NC, T><<<(unsigned)((cells + G - 1) / G), 256, 0, s>>>(P, coarse, fine, cells); \
+    EXG_CUDA(cudaGetLastError());                                                                  \
+    return;                                                                                        \
+  }
+  EXG_TRANSFER_PAIRS(EXG_PROLONG)
+#undef EXG_PROLONG
+  throw Error{EXG_ERR_UNSUPPORTED, "unsupported transfer degree pair"};
 }
 template <class T>
 void restrict_add(const TransferParams& P, const T* fine, T* coarse, cudaStream_t s) {
-  long long n = (long long)P.Nc[0] * P.Nc[1] * P.Nc[2] * P.nc * P.nc * P.nc;
-  restrict_kernel<T><<<(unsigned)((n + 255) / 256), 256, 0, s>>>(P, fine, coarse, n);
-  EXG_CUDA(cudaGetLastError());
+  long long cells = (long long)P.Nc[0] * P.Nc[1] * P.Nc[2];
+#define EXG_RESTRICT(NF, NC)                                                                       \
+  if (P.nf == NF && P.nc == NC) {                                                                  \
+    constexpr int G = TransferShape<NF>::G;                                                        \
+    restrict_kernel<NF, NC, T><<<(unsigned)((cells + G - 1) / G), 256, 0, s>>>(P, fine, coarse, cells); \
+    EXG_CUDA(cudaGetLastError());                                                                  \
+    return;                                                                                        \
+  }
+  EXG_TRANSFER_PAIRS(EXG_RESTRICT)
+#undef EXG_RESTRICT
+  throw Error{EXG_ERR_UNSUPPORTED, "unsupported transfer degree pair"};
 }
 
 // ------------------------------------------------------------------------------------------------
 // coarse CG + point Jacobi in one CTA (MGCoarseKrylov, coarse_grid_solvers.h:157-224).  The dense
 // coarse matrix is assembled at setup.  Iterations are bounded by max_iter.
 // ------------------------------------------------------------------------------------------------
+// block sum in FP64, valid in all threads; sh holds 33 values.  FP64 arithmetic runs at a small
+// fraction of the FP32 rate on this part, so the partial sums are combined by warp 0 alone (one
+// shuffle tree per warp, one for the warp partials) rather than redundantly by every thread.
 __device__ __forceinline__ double cta_sum(double v, double* sh) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-  int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
   __syncthreads();
   if (l == 0) sh[w] = v;
   __syncthreads();
-  double r = 0;
-  for (int i = 0; i < (int)(blockDim.x >> 5); ++i) r += sh[i];
-  return r;  // valid in all threads
+  if (w == 0) {
+    double t = l < nw ? sh[l] : 0.0;
+    for (int o = 16; o > 0; o >>= 1) t += __shfl_down_sync(0xffffffffu, t, o);
+    if (l == 0) sh[32] = t;
+  }
+  __syncthreads();
+  return sh[32];
+}
+
+// out = A in with one warp per row (A symmetric, so row i is read contiguously; lane-strided
+// partial sums reduced by a fixed shuffle tree: deterministic)
+template <class CT>
+__device__ __forceinline__ void coarse_matvec(const CT* A, const CT* in, CT* out, int n) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  for (int i = warp; i < n; i += nw) {
+    const CT* Ai = A + (long long)i * n;
+    CT acc = 0;
+    for (int j = lane; j < n; j += 32) acc += Ai[j] * in[j];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) out[i] = acc;
+  }
+  __syncthreads();
 }
 
 template <class T, class CT>
-__global__ void coarse_cg_kernel(const CT* __restrict__ A, const CT* __restrict__ invd, const T* __restrict__ rhs,
-                                 T* __restrict__ xout, CT* __restrict__ xstate, int n, double rel_tol, double abs_tol,
-                                 int max_iter, int singular, long long* __restrict__ its_counter) {
+__global__ void __launch_bounds__(1024) coarse_cg_kernel(const CT* __restrict__ A, const CT* __restrict__ invd,
+                                                         const T* __restrict__ rhs, T* __restrict__ xout,
+                                                         CT* __restrict__ xstate, int n, double rel_tol,
+                                                         double abs_tol, int max_iter, int singular, int stage_matrix,
+                                                         long long* __restrict__ its_counter) {
   extern __shared__ __align__(16) unsigned char sm[];
   CT* x = reinterpret_cast<CT*>(sm);
   CT* r = x + n;
   CT* z = r + n;
   CT* p = z + n;
   CT* v = p + n;
-  __shared__ double sh[32];
+  CT* As = v + n;  // n*n copy of the matrix when it fits in shared memory
+  __shared__ double sh[33];
+  __shared__ int s_nonzero;
   const int tid = threadIdx.x, nt = blockDim.x;
+  const CT* Am = A;
+  if (stage_matrix) {
+    for (long long e = tid; e < (long long)n * n; e += nt) As[e] = A[e];
+    Am = As;
+  }
+  if (tid == 0) s_nonzero = 0;
   // r = src (mean removed if singular)
   double mean = 0;
   if (singular) {
@@ -317,24 +446,23 @@ __global__ void coarse_cg_kernel(const CT* __restrict__ A, const CT* __restrict_
     for (int i = tid; i < n; i += nt) s += (double)rhs[i];
     mean = cta_sum(s, sh) / n;
   }
+  __syncthreads();
   for (int i = tid; i < n; i += nt) {
     x[i] = xstate[i];
     z[i] = (CT)((double)rhs[i] - mean);  // b
+    if (x[i] != CT(0)) s_nonzero = 1;
   }
   __syncthreads();
   // r = b - A x
-  bool xzero = true;
-  for (int i = 0; i < n; ++i)
-    if (x[i] != CT(0)) {
-      xzero = false;
-      break;
-    }
+  if (s_nonzero) {
+    coarse_matvec(Am, x, v, n);
+  } else {
+    for (int i = tid; i < n; i += nt) v[i] = 0;
+    __syncthreads();
+  }
   double rr = 0;
   for (int i = tid; i < n; i += nt) {
-    CT s = 0;
-    if (!xzero)
-      for (int j = 0; j < n; ++j) s += A[(long long)j * n + i] * x[j];  // A symmetric: coalesced columns
-    r[i] = z[i] - s;
+    r[i] = z[i] - v[i];
     rr += (double)r[i] * (double)r[i];
   }
   double rn = sqrt(cta_sum(rr, sh));
@@ -352,13 +480,9 @@ __global__ void coarse_cg_kernel(const CT* __restrict__ A, const CT* __restrict_
     double beta = it == 1 ? 0.0 : rho / rho_old;
     for (int i = tid; i < n; i += nt) p[i] = it == 1 ? z[i] : z[i] + (CT)beta * p[i];
     __syncthreads();
+    coarse_matvec(Am, p, v, n);
     double pv = 0;
-    for (int i = tid; i < n; i += nt) {
-      CT s = 0;
-      for (int j = 0; j < n; ++j) s += A[(long long)j * n + i] * p[j];
-      v[i] = s;
-      pv += (double)p[i] * (double)s;
-    }
+    for (int i = tid; i < n; i += nt) pv += (double)p[i] * (double)v[i];
     pv = cta_sum(pv, sh);
     double alpha = rho / pv;
     double rr2 = 0;
@@ -381,14 +505,19 @@ __global__ void coarse_cg_kernel(const CT* __restrict__ A, const CT* __restrict_
 template <class T, class CT>
 void coarse_cg(const CT* A, const CT* invd, const T* rhs, T* x, CT* xstate, int n, double rel_tol, double abs_tol,
                int max_iter, int singular, long long* its, cudaStream_t s) {
-  size_t smem = 5 * (size_t)n * sizeof(CT);
+  size_t vec_bytes = 5 * (size_t)n * sizeof(CT), mat_bytes = (size_t)n * n * sizeof(CT);
+  const int stage = vec_bytes + mat_bytes <= 200 * 1024 ? 1 : 0;
+  size_t smem = vec_bytes + (stage ? mat_bytes : 0);
   auto k = coarse_cg_kernel<T, CT>;
   static int attr_bytes = 0;
   if ((int)smem > attr_bytes) {
     EXG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_bytes = (int)smem;
   }
-  k<<<1, 1024, smem, s>>>(A, invd, rhs, x, xstate, n, rel_tol, abs_tol, max_iter, singular, its);
+  // one thread per unknown (whole warps, at most 1024): idle threads would only add FP64 work to
+  // every block reduction
+  const int threads = std::min(1024, std::max(32, (n + 31) / 32 * 32));
+  k<<<1, threads, smem, s>>>(A, invd, rhs, x, xstate, n, rel_tol, abs_tol, max_iter, singular, stage, its);
   EXG_CUDA(cudaGetLastError());
 }
 

@@ -118,6 +118,9 @@ typedef struct {
   int min_coarse_cells;    /* stop h-coarsening at this many cells per direction (2) */
   int singular;            /* subtract the mean in the coarse solve (coarse_grid_solvers.h:161-162) */
   int use_graph;           /* capture the V-cycle as one CUDA graph */
+  int fuse_smoother;       /* 1: Chebyshev steps and the level residual are computed in the operator
+                            * kernels' store (deal.II's pre/post-loop operations of a Chebyshev
+                            * vmult); 0: separate vector kernels.  Both give the same iterates. */
 } exg_mg_desc;
 
 typedef struct {

@@ -55,9 +55,10 @@ def test_mg_levels_and_eigenvalues(mg_prec):
             assert g["lambda_max"] == pytest.approx(o["lambda_max"], rel=1e-9 if mg_prec == E.PREC_F64 else 1e-4)
 
 
-def test_vcycle_matches_oracle_double():
+@pytest.mark.parametrize("curved", [False, True])
+def test_vcycle_matches_oracle_double(curved):
     torch = require_gpu()
-    p, m = sine(3, True)
+    p, m = sine(3, curved)
     op = E.LaplaceOperator(m, 3)
     mg = E.MultigridPreconditioner(op, mg_precision=E.PREC_F64)
     omg = O.Multigrid(p, mg_float=0)
@@ -65,6 +66,26 @@ def test_vcycle_matches_oracle_double():
         r = splitmix_uniform(p.n_dofs, seed)
         z = mg.vmult(op.initialize_dof_vector(), to_dev(torch, r))
         assert rel(z.cpu().numpy(), omg.vmult(r)) <= 1e-9
+
+
+@pytest.mark.parametrize("curved", [False, True])
+@pytest.mark.parametrize("mg_prec", [E.PREC_F64, E.PREC_F32])
+def test_fused_smoother_and_graph_replay(curved, mg_prec):
+    """Chebyshev steps and level residuals fused into the operator kernels, replayed as a CUDA
+    graph, give the iterates of the separate vector kernels run eagerly, over a sequence of
+    V-cycles (the coarse solver starts from its previous solution)."""
+    torch = require_gpu()
+    k = 4 if not curved else 3
+    _, m = sine(k, curved, n=6)
+    op = E.LaplaceOperator(m, k)
+    fused = E.MultigridPreconditioner(op, mg_precision=mg_prec, fuse_smoother=True, use_graph=True)
+    plain = E.MultigridPreconditioner(op, mg_precision=mg_prec, fuse_smoother=False, use_graph=False)
+    tol = 1e-12 if mg_prec == E.PREC_F64 else 1e-5
+    for seed in (3, 4, 5):
+        r = to_dev(torch, splitmix_uniform(op.n_dofs, seed))
+        a = fused.vmult(op.initialize_dof_vector(), r)
+        b = plain.vmult(op.initialize_dof_vector(), r)
+        assert float(torch.linalg.norm(a - b) / torch.linalg.norm(b)) <= tol
 
 
 @pytest.mark.parametrize("curved", [False, True])

@@ -426,6 +426,61 @@ def run_solve(args):
     return 0
 
 
+def run_component(args):
+    """Profiling entry points (not the headline): `--mode operator` times one operator apply
+    (Cartesian or, with --curved, the deformed cube of the curved configuration) and `--mode vcycle`
+    one FP32 V-cycle of the mixed-precision solver.  The timed launches are bracketed by
+    cudaProfilerStart/Stop, so `ncu --profile-from-start off` captures exactly them."""
+    import torch
+
+    import exadg_gb300 as E
+    from exadg_gb300 import build as B
+    from exadg_gb300 import driver as D
+
+    B.build()
+    E.load_library()
+    precs = {"f64": E.PREC_F64, "f32": E.PREC_F32, "f64e": E.PREC_F64E}
+    n, k = args.n_cells, args.degree
+    kw = D.deformed_unit_cube(n, degree=k) if args.curved else D.unit_cube(n)
+    mesh = E.Mesh(**kw)
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    if args.mode == "operator":
+        op = E.LaplaceOperator(mesh, k, 1.0, precs[args.precision])
+        if op.cartesian and not args.no_tune:
+            op.tune()
+        x = torch.tensor(splitmix_uniform(op.n_dofs, 1), device="cuda").to(op.dtype)
+        y = torch.empty_like(x)
+        run = lambda: op.vmult(y, x)
+        what = {"precision": args.precision}
+    else:
+        op = E.LaplaceOperator(mesh, k, 1.0, E.PREC_F64E)
+        if op.cartesian:
+            op.tune()
+        mg = E.MultigridPreconditioner(op, mg_precision=E.PREC_F32)
+        r = torch.tensor(splitmix_uniform(op.n_dofs, 1), device="cuda")
+        z = torch.empty_like(r)
+        run = lambda: mg.vmult(z, r)
+        info = mg.info()
+        what = {"levels": [(l["n_cells"][0], l["degree"]) for l in info["levels"]], "mg_precision": "f32"}
+    for _ in range(max(args.warmup, 3)):
+        run()
+    torch.cuda.synchronize()
+    torch.cuda.profiler.start()
+    e0.record(s)
+    for _ in range(args.steps):
+        run()
+    e1.record(s)
+    e1.synchronize()
+    torch.cuda.profiler.stop()
+    ms = e0.elapsed_time(e1) / args.steps
+    line = {"mode": args.mode, "workload": "%s %d^3 cells, k=%d" % ("curved" if args.curved else "cartesian", n, k),
+            "n_dofs": op.n_dofs, "ms": ms, "dofs_per_s": op.n_dofs / (ms * 1e-3), "steps": args.steps}
+    line.update(what)
+    print(json.dumps(line))
+    return 0
+
+
 def run_learned(args):
     """Pressure-Poisson sequence of the Taylor-Green vortex (32^3 cells, k_p = 2, periodic, Re 1600):
     CG (FP64, FP32-pair operator) + FP32 multigrid to ||r|| <= 1e-10 ||b||, seeded by BDF2
@@ -502,7 +557,8 @@ def main():
     ap.add_argument("--launch-config", type=int, default=None, help="force a launch variant (profiling)")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-solve", action="store_true")
-    ap.add_argument("--mode", default="apply", choices=["apply", "solve", "sweep", "learned"])
+    ap.add_argument("--mode", default="apply", choices=["apply", "solve", "sweep", "learned", "operator", "vcycle"])
+    ap.add_argument("--curved", action="store_true", help="operator / vcycle modes: deformed-cube mesh")
     ap.add_argument("--learned-steps", type=int, default=400)
     ap.add_argument("--learned-epochs", type=int, default=40)
     ap.add_argument("--learned-diagnostics", action="store_true")
@@ -514,6 +570,8 @@ def main():
         return run_solve(args)
     if args.mode == "learned":
         return run_learned(args)
+    if args.mode in ("operator", "vcycle"):
+        return run_component(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)

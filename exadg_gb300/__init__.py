@@ -110,12 +110,14 @@ class CGResult(ctypes.Structure):
 # every symbol declared in include/exadg_gb300.h
 EXPORTED_SYMBOLS = [
     "exg_mesh_create", "exg_mesh_destroy", "exg_sipg_create", "exg_sipg_destroy", "exg_sipg_n_dofs",
-    "exg_sipg_info", "exg_sipg_tune", "exg_sipg_set_launch_config", "exg_sipg_apply_f64", "exg_sipg_apply_f32", "exg_sipg_inverse_diagonal_f64",
+    "exg_sipg_info", "exg_sipg_tune", "exg_sipg_set_launch_config", "exg_sipg_apply_f64", "exg_sipg_apply_f32",
+    "exg_sipg_residual_f64", "exg_sipg_inverse_diagonal_f64",
     "exg_sipg_inverse_diagonal_f32", "exg_sipg_quadrature_points", "exg_sipg_rhs", "exg_mg_default_desc",
     "exg_mg_create", "exg_mg_destroy", "exg_mg_vmult", "exg_mg_info_get", "exg_cg_default_desc", "exg_cg_solve",
     "exg_cg_solve_noalloc", "exg_device_fma_peaks", "exg_status_string", "exg_last_error",
     "exg_cnn_create", "exg_cnn_destroy", "exg_cnn_n_params", "exg_cnn_params", "exg_cnn_forward",
     "exg_cnn_backward", "exg_cnn_train_step", "exg_cnn_adam", "exg_dg_pack", "exg_dg_unpack_add", "exg_dg_pack_diff",
+    "exg_dg_features", "exg_dg_ls_step",
 ]
 
 _lib = None
@@ -145,6 +147,7 @@ def load_library(path=LIB_PATH):
         "exg_sipg_set_launch_config": [P, I],
         "exg_sipg_apply_f64": [P, P, P, I, P],
         "exg_sipg_apply_f32": [P, P, P, I, P],
+        "exg_sipg_residual_f64": [P, P, P, P, P],
         "exg_sipg_inverse_diagonal_f64": [P, P, P],
         "exg_sipg_inverse_diagonal_f32": [P, P, P],
         "exg_sipg_quadrature_points": [P, P, P, ctypes.POINTER(LL), ctypes.POINTER(LL), P],
@@ -169,6 +172,8 @@ def load_library(path=LIB_PATH):
         "exg_dg_pack": [P, P, I, I, LL, P, P],
         "exg_dg_unpack_add": [P, P, D, I, LL, P, P],
         "exg_dg_pack_diff": [P, P, D, I, LL, P, P],
+        "exg_dg_features": [P, P, P, P, I, LL, P, P, P],
+        "exg_dg_ls_step": [P, P, P, P, LL, P, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)
@@ -286,6 +291,11 @@ class LaplaceOperator:
         return dst
 
     apply = vmult
+
+    def residual(self, r, b, x, stream=None):
+        """r = b - A x in one kernel (FP64-storage operators)."""
+        _check(_lib.exg_sipg_residual_f64(self.h, _ptr(b), _ptr(x), _ptr(r), _stream(stream)))
+        return r
 
     def calculate_inverse_diagonal(self, diag, stream=None):
         f = _lib.exg_sipg_inverse_diagonal_f32 if self.precision == PREC_F32 else _lib.exg_sipg_inverse_diagonal_f64

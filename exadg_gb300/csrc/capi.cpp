@@ -114,6 +114,19 @@ exg_status exg_sipg_apply_f32(exg_op* op, const float* src, float* dst, int n_rh
   EXG_API_END
 }
 
+exg_status exg_sipg_residual_f64(exg_op* op, const double* b, const double* x, double* r, void* stream) {
+  EXG_API_BEGIN
+  EXG_CHECK(op && b && x && r, EXG_ERR_INVALID, "null argument");
+  EXG_CHECK(op->precision != EXG_PREC_F32, EXG_ERR_INVALID, "operator precision is FP32");
+  EXG_CHECK(x != r, EXG_ERR_INVALID, "x and r must not alias");
+  exg::PointEpilogue ep;
+  ep.mode = 4;
+  ep.b = b;
+  ep.out = r;
+  op->apply(x, nullptr, 1, (cudaStream_t)stream, ep);
+  EXG_API_END
+}
+
 exg_status exg_sipg_tune(exg_op* op, int n_rhs, int* launch_config, float* timings_ms, int* n_timings,
                          void* stream) {
   EXG_API_BEGIN

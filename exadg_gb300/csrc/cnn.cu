@@ -18,7 +18,6 @@
 
 namespace exg {
 
-static constexpr int CI_CHUNK = 8;
 static constexpr int CNN_MAX_C = 32;
 
 __device__ __forceinline__ int wrap(int a, int n) { return a < 0 ? a + n : (a >= n ? a - n : a); }
@@ -37,17 +36,22 @@ __device__ __forceinline__ float silu_grad(float v) {
 }
 
 // out[co][c] = act(bias[co] + sum_{ci,t} W[co][ci][t] in[ci][nb(c,t)]); pre keeps the
-// pre-activation for the backward pass.  W layout [co][ci][t]; staged in shared memory per chunk of
-// input channels as [ci][t][co] so that a float4 read serves four output channels.
-template <int K, int COUT>
+// pre-activation for the backward pass.  W layout [co][ci][t].  A thread owns one cell and a group
+// of CONV_CG output channels (blockIdx.y selects the group), so a launch has ceil(cout / CONV_CG)
+// times as many threads as cells.  The group's weights are staged in shared memory per chunk of
+// input channels as [ci][t][co], so two float4 reads serve the eight channels of a tap.
+static constexpr int CONV_CG = 8;
+static constexpr int CONV_CI_CHUNK = 16;
+
+template <int K>
 __global__ void __launch_bounds__(128) conv_fwd_kernel(const float* __restrict__ in, const float* __restrict__ W,
                                                        const float* __restrict__ bias, float* __restrict__ out,
-                                                       float* __restrict__ pre, int cin, int nx, int ny, int nz,
-                                                       int act, int accumulate) {
+                                                       float* __restrict__ pre, int cin, int cout, int nx, int ny,
+                                                       int nz, int act, int accumulate) {
   constexpr int K3 = K * K * K;
-  constexpr int CO4 = (COUT + 3) / 4 * 4;
-  __shared__ __align__(16) float sW[CI_CHUNK * K3 * CO4];
+  __shared__ __align__(16) float sW[CONV_CI_CHUNK * K3 * CONV_CG];
   const int nc = nx * ny * nz;
+  const int co0 = blockIdx.y * CONV_CG;
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   const bool ok = c < nc;
   int x = 0, y = 0, z = 0;
@@ -56,41 +60,48 @@ __global__ void __launch_bounds__(128) conv_fwd_kernel(const float* __restrict__
     y = (c / nx) % ny;
     z = c / (nx * ny);
   }
-  float acc[CO4];
+  int nbr[K3];
 #pragma unroll
-  for (int co = 0; co < CO4; ++co) acc[co] = (co < COUT && bias) ? bias[co] : 0.0f;
-  for (int ci0 = 0; ci0 < cin; ci0 += CI_CHUNK) {
-    const int nci = min(CI_CHUNK, cin - ci0);
+  for (int t = 0; t < K3; ++t) nbr[t] = tap_neighbor<K>(x, y, z, t, nx, ny, nz);
+  float acc[CONV_CG];
+#pragma unroll
+  for (int q = 0; q < CONV_CG; ++q) acc[q] = (co0 + q < cout && bias) ? bias[co0 + q] : 0.0f;
+  for (int ci0 = 0; ci0 < cin; ci0 += CONV_CI_CHUNK) {
+    const int nci = min(CONV_CI_CHUNK, cin - ci0);
     __syncthreads();
-    for (int i = threadIdx.x; i < CI_CHUNK * K3 * CO4; i += blockDim.x) {
-      int co = i % CO4, t = (i / CO4) % K3, cil = i / (CO4 * K3);
-      sW[i] = (co < COUT && cil < nci) ? W[((size_t)co * cin + ci0 + cil) * K3 + t] : 0.0f;
+    for (int i = threadIdx.x; i < CONV_CI_CHUNK * K3 * CONV_CG; i += blockDim.x) {
+      int q = i % CONV_CG, t = (i / CONV_CG) % K3, cil = i / (CONV_CG * K3);
+      int co = co0 + q;
+      sW[i] = (co < cout && cil < nci) ? W[((size_t)co * cin + ci0 + cil) * K3 + t] : 0.0f;
     }
     __syncthreads();
     if (ok) {
       for (int cil = 0; cil < nci; ++cil) {
         const float* src = in + (size_t)(ci0 + cil) * nc;
-#pragma unroll 3
-        for (int t = 0; t < K3; ++t) {
-          const float v = __ldg(src + tap_neighbor<K>(x, y, z, t, nx, ny, nz));
-          const float4* w4 = reinterpret_cast<const float4*>(sW + (cil * K3 + t) * CO4);
+        const float4* w4 = reinterpret_cast<const float4*>(sW + cil * K3 * CONV_CG);
 #pragma unroll
-          for (int q = 0; q < CO4 / 4; ++q) {
-            float4 w = w4[q];
-            acc[4 * q + 0] = fmaf(w.x, v, acc[4 * q + 0]);
-            acc[4 * q + 1] = fmaf(w.y, v, acc[4 * q + 1]);
-            acc[4 * q + 2] = fmaf(w.z, v, acc[4 * q + 2]);
-            acc[4 * q + 3] = fmaf(w.w, v, acc[4 * q + 3]);
-          }
+        for (int t = 0; t < K3; ++t) {
+          const float v = __ldg(src + nbr[t]);
+          const float4 wa = w4[2 * t], wb = w4[2 * t + 1];
+          acc[0] = fmaf(wa.x, v, acc[0]);
+          acc[1] = fmaf(wa.y, v, acc[1]);
+          acc[2] = fmaf(wa.z, v, acc[2]);
+          acc[3] = fmaf(wa.w, v, acc[3]);
+          acc[4] = fmaf(wb.x, v, acc[4]);
+          acc[5] = fmaf(wb.y, v, acc[5]);
+          acc[6] = fmaf(wb.z, v, acc[6]);
+          acc[7] = fmaf(wb.w, v, acc[7]);
         }
       }
     }
   }
   if (ok) {
 #pragma unroll
-    for (int co = 0; co < COUT; ++co) {
-      if (pre) pre[(size_t)co * nc + c] = acc[co];
-      float r = act ? silu(acc[co]) : acc[co];
+    for (int q = 0; q < CONV_CG; ++q) {
+      const int co = co0 + q;
+      if (co >= cout) break;
+      if (pre) pre[(size_t)co * nc + c] = acc[q];
+      float r = act ? silu(acc[q]) : acc[q];
       if (accumulate) r += out[(size_t)co * nc + c];
       out[(size_t)co * nc + c] = r;
     }
@@ -119,15 +130,17 @@ __global__ void conv_wgrad_kernel(const float* __restrict__ in, const float* __r
                                   int nz, int chunk) {
   constexpr int K3 = K * K * K;
   extern __shared__ __align__(16) float sm[];
-  float* sg = sm;                  // [cout][chunk]
-  float* sx = sm + cout * chunk;   // [K3][chunk] for one input channel
+  // rows padded to chunk + 1 floats: the threads of a warp read column l of different rows
+  const int cs = chunk + 1;
+  float* sg = sm;                // [cout][cs]
+  float* sx = sm + cout * cs;    // [K3][cs] for one input channel
   const int nc = nx * ny * nz;
   const int ch = blockIdx.x, ci = blockIdx.y;
   const int c0 = ch * chunk;
   const int ncl = min(chunk, nc - c0);
   for (int i = threadIdx.x; i < cout * chunk; i += blockDim.x) {
     int co = i / chunk, l = i % chunk;
-    sg[i] = l < ncl ? gout[(size_t)co * nc + c0 + l] : 0.0f;
+    sg[co * cs + l] = l < ncl ? gout[(size_t)co * nc + c0 + l] : 0.0f;
   }
   for (int i = threadIdx.x; i < K3 * chunk; i += blockDim.x) {
     int t = i / chunk, l = i % chunk;
@@ -136,20 +149,20 @@ __global__ void conv_wgrad_kernel(const float* __restrict__ in, const float* __r
       int c = c0 + l, x = c % nx, y = (c / nx) % ny, z = c / (nx * ny);
       v = in[(size_t)ci * nc + tap_neighbor<K>(x, y, z, t, nx, ny, nz)];
     }
-    sx[i] = v;
+    sx[t * cs + l] = v;
   }
   __syncthreads();
   for (int pidx = threadIdx.x; pidx < cout * K3; pidx += blockDim.x) {
     int co = pidx / K3, t = pidx % K3;
-    const float* g = sg + co * chunk;
-    const float* xv = sx + t * chunk;
+    const float* g = sg + co * cs;
+    const float* xv = sx + t * cs;
     float s = 0.0f;
     for (int l = 0; l < chunk; ++l) s = fmaf(g[l], xv[l], s);
     gWp[(((size_t)ch * cout + co) * cin + ci) * K3 + t] = s;
   }
   if (ci == 0)
     for (int co = threadIdx.x; co < cout; co += blockDim.x) {
-      const float* g = sg + co * chunk;
+      const float* g = sg + co * cs;
       float s = 0.0f;
       for (int l = 0; l < chunk; ++l) s += g[l];
       gbp[(size_t)ch * cout + co] = s;
@@ -239,6 +252,115 @@ __global__ void pack_diff_kernel(const double* __restrict__ a, const double* __r
 }
 
 // ---------------------------------------------------------------------------------------------------
+// guess assembly without host round trips: feature scaling and the least-squares step length are
+// reduced on the device (per-block partials in a static array, summed in index order by one warp per
+// quantity).  Calls that overlap on the GPU share the partials array and race.
+// ---------------------------------------------------------------------------------------------------
+static constexpr int RED_NB = 608;  // 4 blocks per SM
+__device__ double g_dg_partials[4 * RED_NB];
+
+__device__ __forceinline__ double warp_sum_d(double v) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// partials[j][block] = sum over the block's entries of f_j^2 (NF = 4: features) or of the products
+// (NF = 3: r.Ae, Ae.Ae, r.r)
+template <int NF>
+__global__ void __launch_bounds__(256) dg_partials_kernel(const double* __restrict__ a, const double* __restrict__ b,
+                                                          const double* __restrict__ c, const double* __restrict__ d,
+                                                          long long n) {
+  double acc[NF];
+#pragma unroll
+  for (int j = 0; j < NF; ++j) acc[j] = 0.0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    if constexpr (NF == 4) {  // a = p0, b = p1, c = p2, d = r
+      const double p0 = a[i], p1 = b[i], p2 = c[i], rr = d[i];
+      const double d1 = p0 - p1, d2 = p0 - 2.0 * p1 + p2;
+      acc[0] += p0 * p0;
+      acc[1] += d1 * d1;
+      acc[2] += d2 * d2;
+      acc[3] += rr * rr;
+    } else {  // a = r, b = Ae
+      const double r = a[i], ae = b[i];
+      acc[0] += r * ae;
+      acc[1] += ae * ae;
+      acc[2] += r * r;
+    }
+  }
+  __shared__ double sh[NF][8];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+  for (int j = 0; j < NF; ++j) {
+    double v = warp_sum_d(acc[j]);
+    if (l == 0) sh[j][w] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < NF) {
+    double v = 0.0;
+    for (int k = 0; k < (int)(blockDim.x >> 5); ++k) v += sh[threadIdx.x][k];
+    g_dg_partials[threadIdx.x * RED_NB + blockIdx.x] = v;
+  }
+}
+
+// one warp per quantity: out[j] = sum of partials[j][:] (then mode 0: rms = sqrt(sum / n);
+// mode 1: out = {r.Ae, Ae.Ae, r.r, step}, step = max(r.Ae / Ae.Ae, 0), 0 when not finite)
+__global__ void dg_finalize_kernel(int nq, int mode, long long n, double* __restrict__ out) {
+  __shared__ double tot[4];
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (w < nq) {
+    double v = 0.0;
+    for (int k = l; k < RED_NB; k += 32) v += g_dg_partials[w * RED_NB + k];
+    v = warp_sum_d(v);
+    if (l == 0) tot[w] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    if (mode == 0) {
+      for (int j = 0; j < nq; ++j) out[j] = fmax(sqrt(tot[j] / (double)n), 1e-300);
+    } else {
+      double c = tot[1] > 0.0 ? tot[0] / tot[1] : 0.0;
+      if (!(c > 0.0) || !isfinite(c)) c = 0.0;
+      out[0] = tot[0];
+      out[1] = tot[1];
+      out[2] = tot[2];
+      out[3] = c;
+    }
+  }
+}
+
+// x[j*npc + i][c] = f_j[c*npc + i] / rms_j with f = (p0, p0 - p1, p0 - 2 p1 + p2, r)
+__global__ void dg_features_pack_kernel(const double* __restrict__ p0, const double* __restrict__ p1,
+                                        const double* __restrict__ p2, const double* __restrict__ r,
+                                        const double* __restrict__ rms, int npc, long long n_cells,
+                                        float* __restrict__ x) {
+  long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= 4LL * npc * n_cells) return;
+  long long c = g % n_cells;
+  long long ch = g / n_cells;
+  int j = (int)(ch / npc), i = (int)(ch % npc);
+  long long k = c * npc + i;
+  double v;
+  if (j == 0)
+    v = p0[k];
+  else if (j == 1)
+    v = p0[k] - p1[k];
+  else if (j == 2)
+    v = p0[k] - 2.0 * p1[k] + p2[k];
+  else
+    v = r[k];
+  x[g] = (float)(v / rms[j]);
+}
+
+// x = base + stats[3] e
+__global__ void dg_step_kernel(const double* __restrict__ base, const double* __restrict__ e,
+                               const double* __restrict__ stats, long long n, double* __restrict__ x) {
+  const double c = stats[3];
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    x[i] = base[i] + c * e[i];
+}
+
+// ---------------------------------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------------------------------
 static void* cnn_alloc(size_t bytes) {
@@ -248,32 +370,16 @@ static void* cnn_alloc(size_t bytes) {
   return p;
 }
 
-template <int K, int COUT>
-static void conv_fwd_launch(const float* in, const float* W, const float* b, float* out, float* pre, int cin,
-                            const int N[3], int act, int acc, cudaStream_t s) {
-  int nc = N[0] * N[1] * N[2];
-  conv_fwd_kernel<K, COUT><<<(nc + 127) / 128, 128, 0, s>>>(in, W, b, out, pre, cin, N[0], N[1], N[2], act, acc);
-  EXG_CUDA(cudaGetLastError());
-}
-
 static void conv_fwd(int K, int cout, const float* in, const float* W, const float* b, float* out, float* pre,
                      int cin, const int N[3], int act, cudaStream_t s, int acc = 0) {
   EXG_CHECK(cout >= 1 && cout <= CNN_MAX_C, EXG_ERR_UNSUPPORTED, "conv: at most 32 output channels");
-  if (K == 1) {
-    if (cout <= 16)
-      conv_fwd_launch<1, 16>(in, W, b, out, pre, cin, N, act, acc, s);
-    else if (cout <= 28)
-      conv_fwd_launch<1, 28>(in, W, b, out, pre, cin, N, act, acc, s);
-    else
-      conv_fwd_launch<1, 32>(in, W, b, out, pre, cin, N, act, acc, s);
-  } else {
-    if (cout <= 16)
-      conv_fwd_launch<3, 16>(in, W, b, out, pre, cin, N, act, acc, s);
-    else if (cout <= 28)
-      conv_fwd_launch<3, 28>(in, W, b, out, pre, cin, N, act, acc, s);
-    else
-      conv_fwd_launch<3, 32>(in, W, b, out, pre, cin, N, act, acc, s);
-  }
+  int nc = N[0] * N[1] * N[2];
+  dim3 grid((unsigned)((nc + 127) / 128), (unsigned)((cout + CONV_CG - 1) / CONV_CG));
+  if (K == 1)
+    conv_fwd_kernel<1><<<grid, 128, 0, s>>>(in, W, b, out, pre, cin, cout, N[0], N[1], N[2], act, acc);
+  else
+    conv_fwd_kernel<3><<<grid, 128, 0, s>>>(in, W, b, out, pre, cin, cout, N[0], N[1], N[2], act, acc);
+  EXG_CUDA(cudaGetLastError());
 }
 
 }  // namespace exg
@@ -363,7 +469,7 @@ void exg_cnn::forward(const float* x, float* out, bool keep, cudaStream_t s) {
 
 void exg_cnn::wgrad(int K, const float* in, const float* g, int cin, int cout, float* gW, float* gb, cudaStream_t s) {
   int K3 = K * K * K;
-  size_t smem = ((size_t)cout * chunk + (size_t)K3 * chunk) * 4;
+  size_t smem = ((size_t)cout + K3) * (chunk + 1) * 4;
   static int attr = 0;
   if ((int)smem > attr) {
     EXG_CUDA(cudaFuncSetAttribute(conv_wgrad_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
@@ -540,6 +646,35 @@ exg_status exg_dg_pack_diff(const double* a, const double* b, double inv_scale, 
   long long tot = n_cells * dofs_per_cell;
   pack_diff_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, (cudaStream_t)stream>>>(a, b, inv_scale, dofs_per_cell,
                                                                                     n_cells, t);
+  EXG_CUDA(cudaGetLastError());
+  CNN_END
+}
+
+exg_status exg_dg_features(const double* p0, const double* p1, const double* p2, const double* r,
+                           int dofs_per_cell, long long n_cells, float* x, double* rms, void* stream) {
+  CNN_BEGIN
+  EXG_CHECK(p0 && p1 && p2 && r && x && rms, EXG_ERR_INVALID, "null argument");
+  EXG_CHECK(dofs_per_cell >= 1 && n_cells >= 1, EXG_ERR_INVALID, "empty vectors");
+  cudaStream_t s = (cudaStream_t)stream;
+  const long long n = n_cells * dofs_per_cell;
+  dg_partials_kernel<4><<<RED_NB, 256, 0, s>>>(p0, p1, p2, r, n);
+  dg_finalize_kernel<<<1, 128, 0, s>>>(4, 0, n, rms);
+  const long long tot = 4 * n;
+  dg_features_pack_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(p0, p1, p2, r, rms, dofs_per_cell, n_cells,
+                                                                        x);
+  EXG_CUDA(cudaGetLastError());
+  CNN_END
+}
+
+exg_status exg_dg_ls_step(const double* r, const double* Ae, const double* e, const double* base, long long n,
+                          double* x, double* stats, void* stream) {
+  CNN_BEGIN
+  EXG_CHECK(r && Ae && e && base && x && stats, EXG_ERR_INVALID, "null argument");
+  EXG_CHECK(n >= 1, EXG_ERR_INVALID, "empty vectors");
+  cudaStream_t s = (cudaStream_t)stream;
+  dg_partials_kernel<3><<<RED_NB, 256, 0, s>>>(r, Ae, nullptr, nullptr, n);
+  dg_finalize_kernel<<<1, 128, 0, s>>>(3, 1, n, stats);
+  dg_step_kernel<<<RED_NB * 2, 256, 0, s>>>(base, e, stats, n, x);
   EXG_CUDA(cudaGetLastError());
   CNN_END
 }

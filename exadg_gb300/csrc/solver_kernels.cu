@@ -402,6 +402,36 @@ __device__ __forceinline__ double cta_sum(double v, double* sh) {
   return sh[32];
 }
 
+// two block sums in the coarse precision, valid in all threads; sh holds 66 values
+template <class R>
+__device__ __forceinline__ void cta_sum2(R& a, R& b, R* sh) {
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+  }
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __syncthreads();
+  if (l == 0) {
+    sh[w] = a;
+    sh[32 + w] = b;
+  }
+  __syncthreads();
+  if (w == 0) {
+    R ta = l < nw ? sh[l] : R(0), tb = l < nw ? sh[32 + l] : R(0);
+    for (int o = 16; o > 0; o >>= 1) {
+      ta += __shfl_down_sync(0xffffffffu, ta, o);
+      tb += __shfl_down_sync(0xffffffffu, tb, o);
+    }
+    if (l == 0) {
+      sh[64] = ta;
+      sh[65] = tb;
+    }
+  }
+  __syncthreads();
+  a = sh[64];
+  b = sh[65];
+}
+
 // out = A in with one warp per row (A symmetric, so row i is read contiguously; lane-strided
 // partial sums reduced by a fixed shuffle tree: deterministic)
 template <class CT>
@@ -431,6 +461,7 @@ __global__ void __launch_bounds__(1024) coarse_cg_kernel(const CT* __restrict__ 
   CT* v = p + n;
   CT* As = v + n;  // n*n copy of the matrix when it fits in shared memory
   __shared__ double sh[33];
+  __shared__ CT shc[66];
   __shared__ int s_nonzero;
   const int tid = threadIdx.x, nt = blockDim.x;
   const CT* Am = A;
@@ -460,39 +491,45 @@ __global__ void __launch_bounds__(1024) coarse_cg_kernel(const CT* __restrict__ 
     for (int i = tid; i < n; i += nt) v[i] = 0;
     __syncthreads();
   }
-  double rr = 0;
+  // scalars in the coarse precision CT (deal.II's SolverCG on float vectors reduces in float);
+  // z = D^-1 r is formed with the residual update so that r.r and r.z share one block reduction
+  CT rr = 0, rz = 0;
   for (int i = tid; i < n; i += nt) {
-    r[i] = z[i] - v[i];
-    rr += (double)r[i] * (double)r[i];
+    const CT ri = z[i] - v[i];
+    const CT zi = invd[i] * ri;
+    r[i] = ri;
+    z[i] = zi;
+    rr += ri * ri;
+    rz += ri * zi;
   }
-  double rn = sqrt(cta_sum(rr, sh));
-  const double tol = fmax(abs_tol, rel_tol * rn);
+  cta_sum2(rr, rz, shc);
+  CT rn = sqrt(rr);
+  const CT tol = (CT)fmax(abs_tol, rel_tol * (double)rn);
   int it = 0;
-  double rho_old = 1;
+  CT rho = rz, beta = 0;
   while (rn > tol && it < max_iter) {
     ++it;
-    double rz = 0;
-    for (int i = tid; i < n; i += nt) {
-      z[i] = invd[i] * r[i];
-      rz += (double)r[i] * (double)z[i];
-    }
-    double rho = cta_sum(rz, sh);
-    double beta = it == 1 ? 0.0 : rho / rho_old;
-    for (int i = tid; i < n; i += nt) p[i] = it == 1 ? z[i] : z[i] + (CT)beta * p[i];
+    for (int i = tid; i < n; i += nt) p[i] = it == 1 ? z[i] : z[i] + beta * p[i];
     __syncthreads();
     coarse_matvec(Am, p, v, n);
-    double pv = 0;
-    for (int i = tid; i < n; i += nt) pv += (double)p[i] * (double)v[i];
-    pv = cta_sum(pv, sh);
-    double alpha = rho / pv;
-    double rr2 = 0;
+    CT pv = 0, unused = 0;
+    for (int i = tid; i < n; i += nt) pv += p[i] * v[i];
+    cta_sum2(pv, unused, shc);
+    const CT alpha = rho / pv;
+    CT rr2 = 0, rz2 = 0;
     for (int i = tid; i < n; i += nt) {
-      x[i] += (CT)alpha * p[i];
-      r[i] -= (CT)alpha * v[i];
-      rr2 += (double)r[i] * (double)r[i];
+      x[i] += alpha * p[i];
+      const CT ri = r[i] - alpha * v[i];
+      const CT zi = invd[i] * ri;
+      r[i] = ri;
+      z[i] = zi;
+      rr2 += ri * ri;
+      rz2 += ri * zi;
     }
-    rn = sqrt(cta_sum(rr2, sh));
-    rho_old = rho;
+    cta_sum2(rr2, rz2, shc);
+    rn = sqrt(rr2);
+    beta = rz2 / rho;
+    rho = rz2;
   }
   __syncthreads();
   for (int i = tid; i < n; i += nt) {

@@ -10,11 +10,11 @@ converged pressures every `train_every` steps in the energy norm that CG minimis
 L = (d - e)^T A (d - e) / d^T A d with d = p - p_ext and e = s y(x) (A (d - e) = r_ext - A e, so the
 gradient costs one operator apply).  At inference the correction is scaled by the one-term
 least-squares coefficient c = <r_ext, A e> / ||A e||^2, so the learned guess p_ext + c e never has a
-larger residual than p_ext; whenever it does not have a strictly smaller initial residual the plain
-extrapolation is used (fallback).  Both seedings run FP64 CG + FP32 multigrid to the same
-tolerance, ||r|| <= tol * ||b||.
+larger residual than p_ext (||r_ext - c A e||^2 = ||r_ext||^2 - c <r_ext, A e>); when c is not
+positive the plain extrapolation is used (fallback).  Feature scaling, c and the fallback are
+computed on the device, so building the guess needs no host round trip.  Both seedings run FP64
+CG + FP32 multigrid to the same tolerance, ||r|| <= tol * ||b||.
 """
-import ctypes
 import time
 
 import exadg_gb300 as E
@@ -64,31 +64,34 @@ class PressureSequence:
         self.log = []
         n = self.op.n_dofs
         self.tmp = torch.empty(n, dtype=torch.float64, device="cuda")
-        self.ptrs = torch.empty(4, dtype=torch.int64, device="cuda")
-        self.inv_scales = torch.empty(4, dtype=torch.float64, device="cuda")
+        self.zero = torch.zeros(n, dtype=torch.float64, device="cuda")
+        self.e = torch.empty(n, dtype=torch.float64, device="cuda")
+        self.Ae = torch.empty(n, dtype=torch.float64, device="cuda")
+        self.rms = torch.empty(4, dtype=torch.float64, device="cuda")
         self.diagnostics = False
 
     # ------------------------------------------------------------------------------------------
     def _residual(self, b, x):
-        self.op.vmult(self.tmp, x)
-        return b - self.tmp
+        return self.op.residual(self.torch.empty_like(x), b, x)
+
+    def _extrapolation(self):
+        """BDF2 extrapolation 2 p^n - p^{n-1} (one kernel)."""
+        return self.torch.lerp(self.hist[-2], self.hist[-1], 2.0)
 
     def _features(self, b, p_ext):
-        torch = self.torch
-        p0, p1, p2 = self.hist[-1], self.hist[-2], self.hist[-3]
-        d1 = p0 - p1
-        d2 = p0 - 2 * p1 + p2
-        r = self._residual(b, p_ext)
-        vecs = [p0, d1, d2, r]
-        sc = [max(_rms(v), 1e-300) for v in vecs]
-        self.ptrs.copy_(torch.tensor([v.data_ptr() for v in vecs], dtype=torch.int64))
-        self.inv_scales.copy_(torch.tensor([1.0 / s for s in sc], dtype=torch.float64))
-        E._check(E._lib.exg_dg_pack(ctypes.c_void_p(self.ptrs.data_ptr()), ctypes.c_void_p(self.inv_scales.data_ptr()),
-                                    4, self.dpc, self.nc, E._ptr(self.x), E._stream()))
-        return vecs  # keep tensors alive until the pack has run
+        """Network input from (p^n, p^n - p^{n-1}, p^n - 2 p^{n-1} + p^{n-2}, b - A p_ext), each scaled
+        by its RMS on the device; returns r_ext = b - A p_ext.  No host round trip."""
+        r_ext = self.torch.empty_like(p_ext)
+        self.op.residual(r_ext, b, p_ext)
+        E._check(E._lib.exg_dg_features(E._ptr(self.hist[-1]), E._ptr(self.hist[-2]), E._ptr(self.hist[-3]),
+                                        E._ptr(r_ext), self.dpc, self.nc, E._ptr(self.x), E._ptr(self.rms),
+                                        E._stream()))
+        return r_ext
 
     def initial_guess(self, b):
-        """Returns (guess, info)."""
+        """Returns (guess, info).  The learned branch runs without a host round trip: the step length
+        of the correction and the fallback decision are taken on the device (exg_dg_ls_step); the
+        statistics behind them are read after the solve (info["stats"])."""
         torch = self.torch
         info = {"source": "zero"}
         if len(self.hist) == 0:
@@ -96,43 +99,46 @@ class PressureSequence:
         if len(self.hist) == 1:
             info["source"] = "previous"
             return self.hist[-1].clone(), info
-        p_ext = 2 * self.hist[-1] - self.hist[-2]
+        p_ext = self._extrapolation()
         info["source"] = "extrapolation"
         if self.cnn is None or len(self.hist) < 3 or not self.trained or self.delta_scale is None:
             return p_ext, info
-        keep = self._features(b, p_ext)
-        r_ext = keep[3]
+        r_ext = self._features(b, p_ext)
         y = self.cnn.forward(self.x)
-        e = torch.empty_like(p_ext)
-        E._check(E._lib.exg_dg_unpack_add(E._ptr(y), E._ptr(torch.zeros_like(p_ext)), self.delta_scale, self.dpc,
-                                          self.nc, E._ptr(e), E._stream()))
-        Ae = torch.empty_like(p_ext)
-        self.op.vmult(Ae, e)
-        aa = float(Ae @ Ae)
-        c = float(r_ext @ Ae) / aa if aa > 0 else 0.0
-        r_ext_n = float(torch.linalg.norm(r_ext))
-        r_cnn_n = float(torch.linalg.norm(r_ext - c * Ae))
-        info.update(r_ext=r_ext_n, r_cnn=r_cnn_n, c=c)
+        E._check(E._lib.exg_dg_unpack_add(E._ptr(y), E._ptr(self.zero), self.delta_scale, self.dpc, self.nc,
+                                          E._ptr(self.e), E._stream()))
+        self.op.vmult(self.Ae, self.e)
+        x = torch.empty_like(p_ext)
+        stats = torch.empty(4, dtype=torch.float64, device="cuda")
+        E._check(E._lib.exg_dg_ls_step(E._ptr(r_ext), E._ptr(self.Ae), E._ptr(self.e), E._ptr(p_ext),
+                                       self.op.n_dofs, E._ptr(x), E._ptr(stats), E._stream()))
+        info["stats"] = stats
         if self.diagnostics:  # residual of the third-order extrapolation p_ext + (p^n - 2p^{n-1} + p^{n-2})
-            info["r_ext3"] = float(torch.linalg.norm(self._residual(b, p_ext + keep[2])))
-        del keep
-        if c > 0 and r_cnn_n < r_ext_n:
-            info["source"] = "learned"
-            return p_ext + c * e, info
-        info["source"] = "fallback"
-        return p_ext, info
+            d2 = self.hist[-1] - 2 * self.hist[-2] + self.hist[-3]
+            info["r_ext3"] = float(torch.linalg.norm(self._residual(b, p_ext + d2)))
+        return x, info
+
+    @staticmethod
+    def _resolve(info):
+        """Reads the device statistics of a learned guess (after the solve has synchronised)."""
+        if "stats" not in info:
+            return info
+        rae, aa, rr, c = info.pop("stats").tolist()
+        info["c"] = c
+        info["r_ext"] = rr ** 0.5
+        info["r_cnn"] = max(rr - c * rae, 0.0) ** 0.5
+        info["source"] = "learned" if c > 0 else "fallback"
+        return info
 
     def _record_sample(self, b, p_new):
         """Training sample: features at the state before the solve and r_ext = b - A p_ext."""
         if self.cnn is None or len(self.hist) < 3:
             return
-        p_ext = 2 * self.hist[-1] - self.hist[-2]
-        keep = self._features(b, p_ext)
+        p_ext = self._extrapolation()
+        r_ext = self._features(b, p_ext)
         delta = p_new - p_ext
         s = _rms(delta)
         self.delta_scale = s if self.delta_scale is None else 0.8 * self.delta_scale + 0.2 * s
-        r_ext = keep[3].clone()
-        del keep
         self.samples.append((self.x.clone(), r_ext, delta))
         if len(self.samples) > self.buffer_size:
             self.samples.pop(0)
@@ -178,6 +184,7 @@ class PressureSequence:
         x -= x.mean()  # fix the pressure level of the singular problem
         torch.cuda.synchronize()
         t2 = time.perf_counter()
+        info = self._resolve(info)
         rec = dict(step=len(self.log), iterations=its, solve_s=t2 - t1, guess_s=t1 - t0, source=info["source"],
                    r0_rel=solver.result["r0"] / bn)
         if "r_ext" in info:

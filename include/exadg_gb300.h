@@ -76,6 +76,9 @@ exg_status exg_sipg_info(const exg_op* op, int* degree, int* precision, int* car
  * EXG_PREC_F32 operators. */
 exg_status exg_sipg_apply_f64(exg_op* op, const double* src, double* dst, int n_rhs, void* stream);
 exg_status exg_sipg_apply_f32(exg_op* op, const float* src, float* dst, int n_rhs, void* stream);
+/* r = b - A x in one kernel (the residual step of the V-cycle and of its residual check,
+ * multigrid/multigrid_algorithm.h:155-160, 215-216); r must not alias x.  FP64 storage operators. */
+exg_status exg_sipg_residual_f64(exg_op* op, const double* b, const double* x, double* r, void* stream);
 
 /* Autotuner: times the launch variants of the apply kernel (cells per thread block; one thread
  * per line of a cell) for this operator's degree, precision and n_rhs, keeps the fastest and
@@ -195,6 +198,20 @@ exg_status exg_dg_pack(const double* const* vecs, const double* inv_scales, int 
 /* dst[c*dpc + i] = base[c*dpc + i] + scale * y[i][c] */
 exg_status exg_dg_unpack_add(const float* y, const double* base, double scale, int dofs_per_cell,
                              long long n_cells, double* dst, void* stream);
+/* Network input of the learned guess, all on the device: the four features
+ * f = (p0, p0 - p1, p0 - 2 p1 + p2, r) of the DG vectors p0, p1, p2 (newest first) and r, each
+ * divided by its root mean square over the DoFs, x[j*dpc + i][c] = f_j[c*dpc + i] / rms[j];
+ * rms (4 device doubles) is written too. */
+exg_status exg_dg_features(const double* p0, const double* p1, const double* p2, const double* r,
+                           int dofs_per_cell, long long n_cells, float* x, double* rms, void* stream);
+/* Least-squares step along a correction e with Ae = A e, without a host round trip:
+ * stats = {r.Ae, Ae.Ae, r.r, c} with c = max(r.Ae / Ae.Ae, 0) (0 if not finite) and x = base + c e.
+ * With r = b - A base, the residual of x is r - c Ae, of squared norm r.r - c r.Ae <= r.r: c = 0
+ * (plain base) is the fallback when the correction does not reduce the residual.  Calls that
+ * overlap on the GPU race (shared reduction array); this and exg_dg_features add no counterpart
+ * to the reference. */
+exg_status exg_dg_ls_step(const double* r, const double* Ae, const double* e, const double* base, long long n,
+                          double* x, double* stats, void* stream);
 /* t[i][c] = (a[c*dpc + i] - b[c*dpc + i]) * inv_scale */
 exg_status exg_dg_pack_diff(const double* a, const double* b, double inv_scale, int dofs_per_cell,
                             long long n_cells, float* t, void* stream);

@@ -44,6 +44,20 @@ def test_apply_f32(kind, k):
     assert rel(y.cpu().numpy(), p.apply(x.astype(np.float64))) <= 1e-5
 
 
+@pytest.mark.parametrize("prec", [E.PREC_F64, E.PREC_F64E])
+@pytest.mark.parametrize("kind", ["mixed", "periodic", "curved"])
+@pytest.mark.parametrize("k", [2, 5])
+def test_residual_fused(prec, kind, k):
+    """r = b - A x from the operator's fused store against the oracle's A x."""
+    torch = require_gpu()
+    p, m, op = pair(kind, 3, k, prec)
+    x = splitmix_uniform(p.n_dofs, 11)
+    b = splitmix_uniform(p.n_dofs, 12)
+    r = op.residual(op.initialize_dof_vector(), to_dev(torch, b), to_dev(torch, x))
+    ref = b - p.apply(x)
+    assert rel(r.cpu().numpy(), ref) <= 1e-12
+
+
 @pytest.mark.parametrize("prec", [E.PREC_F64, E.PREC_F32, E.PREC_F64E])
 @pytest.mark.parametrize("k", [2, 4])
 def test_apply_multi_rhs(prec, k):

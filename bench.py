@@ -20,6 +20,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 N_CELLS = 64
+E2E_SLABS = 8  # z-slabs of the pipelined host-vector apply
 DEGREE = 4
 METRIC = "DoF/s of op apply (FP64 SIPG Laplace, k=4, 64^3 cells)"
 UNIT = "DoF/s"
@@ -232,22 +233,30 @@ def run_gpu(args):
     value = job_throughput(n, ms * 1e-3, world)
     y_ref = y.double().clone()
 
-    # e2e: host input -> device -> apply -> host output, every step
+    # e2e: host input -> device -> apply -> host output, every step, through the host-vector entry
+    # point (exg_sipg_apply_host_f64: copies pipelined against the apply by z-slabs); FP32 operators
+    # copy and apply in sequence
+    if prec != E.PREC_F32:
+        def e2e_step():
+            op.vmult_host(y_host, x_host, n_slabs=E2E_SLABS)
+    else:
+        def e2e_step():
+            x.copy_(x_host, non_blocking=True)
+            op.vmult(y, x)
+            y_host.copy_(y, non_blocking=True)
     for _ in range(2):
-        x.copy_(x_host, non_blocking=True)
-        op.vmult(y, x)
-        y_host.copy_(y, non_blocking=True)
+        e2e_step()
     barrier()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e2e_steps = max(3, args.steps // 10)
     e0.record(stream)
     for _ in range(e2e_steps):
-        x.copy_(x_host, non_blocking=True)
-        op.vmult(y, x)
-        y_host.copy_(y, non_blocking=True)
+        e2e_step()
     e1.record(stream)
     barrier()
     e2e_ms = max_over_ranks(e0.elapsed_time(e1) / e2e_steps)
+    torch.cuda.synchronize()
+    e2e_rel_diff = float(torch.linalg.norm(y_host.cuda().double() - y.double()) / torch.linalg.norm(y.double()))
 
     pk = peaks()
     bytes_per_apply = 2.0 * esize * n
@@ -275,7 +284,10 @@ def run_gpu(args):
                          "note": "of measured; algorithmic bytes = 2 x %d B x n_dofs per apply; traffic = ncu DRAM "
                                  "read+write of the 48^3 capture scaled by DoF" % esize},
             "e2e": {"value": world * n / (e2e_ms * 1e-3), "unit": UNIT, "h2d_bytes_per_step": esize * n,
-                    "d2h_bytes_per_step": esize * n},
+                    "d2h_bytes_per_step": esize * n, "ms_per_step": e2e_ms,
+                    "path": ("exg_sipg_apply_host_f64, %d z-slabs, pinned host vectors" % E2E_SLABS)
+                    if prec != E.PREC_F32 else "copy in, exg_sipg_apply_f32, copy out",
+                    "rel_diff_vs_device_apply": e2e_rel_diff},
             "gpu_launches": args.steps,
             "clocks": clk.summary(),
             "device_fma_peaks_tflops": {"f64": f64_tf, "f32": f32_tf},

@@ -111,7 +111,7 @@ class CGResult(ctypes.Structure):
 EXPORTED_SYMBOLS = [
     "exg_mesh_create", "exg_mesh_destroy", "exg_sipg_create", "exg_sipg_destroy", "exg_sipg_n_dofs",
     "exg_sipg_info", "exg_sipg_tune", "exg_sipg_set_launch_config", "exg_sipg_apply_f64", "exg_sipg_apply_f32",
-    "exg_sipg_residual_f64", "exg_sipg_inverse_diagonal_f64",
+    "exg_sipg_residual_f64", "exg_sipg_apply_host_f64", "exg_sipg_inverse_diagonal_f64",
     "exg_sipg_inverse_diagonal_f32", "exg_sipg_quadrature_points", "exg_sipg_rhs", "exg_mg_default_desc",
     "exg_mg_create", "exg_mg_destroy", "exg_mg_vmult", "exg_mg_info_get", "exg_cg_default_desc", "exg_cg_solve",
     "exg_cg_solve_noalloc", "exg_device_fma_peaks", "exg_status_string", "exg_last_error",
@@ -148,6 +148,7 @@ def load_library(path=LIB_PATH):
         "exg_sipg_apply_f64": [P, P, P, I, P],
         "exg_sipg_apply_f32": [P, P, P, I, P],
         "exg_sipg_residual_f64": [P, P, P, P, P],
+        "exg_sipg_apply_host_f64": [P, P, P, I, P],
         "exg_sipg_inverse_diagonal_f64": [P, P, P],
         "exg_sipg_inverse_diagonal_f32": [P, P, P],
         "exg_sipg_quadrature_points": [P, P, P, ctypes.POINTER(LL), ctypes.POINTER(LL), P],
@@ -202,6 +203,14 @@ def _ptr(t):
         raise ExgError(EXG_ERR_INVALID, "expected a CUDA tensor")
     if not t.is_contiguous():
         raise ExgError(EXG_ERR_INVALID, "expected a contiguous tensor")
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _host_ptr(t, dtype_name="float64"):
+    import torch
+
+    if not isinstance(t, torch.Tensor) or t.is_cuda or not t.is_contiguous() or t.dtype != getattr(torch, dtype_name):
+        raise ExgError(EXG_ERR_INVALID, "expected a contiguous host %s tensor" % dtype_name)
     return ctypes.c_void_p(t.data_ptr())
 
 
@@ -291,6 +300,13 @@ class LaplaceOperator:
         return dst
 
     apply = vmult
+
+    def vmult_host(self, dst_host, src_host, n_slabs=8, stream=None):
+        """dst_host = A src_host for FP64 host tensors (pinned for copy/compute overlap); queued on
+        `stream`, complete when it synchronises."""
+        _check(_lib.exg_sipg_apply_host_f64(self.h, _host_ptr(src_host), _host_ptr(dst_host), n_slabs,
+                                            _stream(stream)))
+        return dst_host
 
     def residual(self, r, b, x, stream=None):
         """r = b - A x in one kernel (FP64-storage operators)."""

@@ -114,6 +114,16 @@ exg_status exg_sipg_apply_f32(exg_op* op, const float* src, float* dst, int n_rh
   EXG_API_END
 }
 
+exg_status exg_sipg_apply_host_f64(exg_op* op, const double* src_host, double* dst_host, int n_slabs,
+                                   void* stream) {
+  EXG_API_BEGIN
+  EXG_CHECK(op && src_host && dst_host, EXG_ERR_INVALID, "null argument");
+  EXG_CHECK(src_host != dst_host, EXG_ERR_INVALID, "src and dst must not alias");
+  EXG_CHECK(n_slabs >= 1, EXG_ERR_INVALID, "n_slabs must be >= 1");
+  op->apply_host(src_host, dst_host, n_slabs, (cudaStream_t)stream);
+  EXG_API_END
+}
+
 exg_status exg_sipg_residual_f64(exg_op* op, const double* b, const double* x, double* r, void* stream) {
   EXG_API_BEGIN
   EXG_CHECK(op && b && x && r, EXG_ERR_INVALID, "null argument");

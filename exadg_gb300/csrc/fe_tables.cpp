@@ -166,6 +166,8 @@ void build_cart_host(const MeshInfo& m, const FE1D& fe, double ip, CartHost& out
   for (int f = 0; f < 6; ++f) out.mesh.bc[f] = m.d.bc[f];
   out.mesh.n_cells = m.n_cells();
   out.mesh.n_dofs = m.n_cells() * n * n * n;
+  out.mesh.cell_begin = 0;
+  out.mesh.cell_end = out.mesh.n_cells;
 }
 
 }  // namespace exg

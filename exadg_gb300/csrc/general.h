@@ -22,8 +22,9 @@ struct GeneralGeom {
   void build(const MeshInfo& m, const FE1D& fe, double ip, int precision, bool keep_raw, cudaStream_t s);
 };
 
+// cells [cell_begin, cell_end) are written (cell_end < 0: to the last cell)
 void general_apply(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s,
-                   const PointEpilogue& ep = PointEpilogue());
+                   const PointEpilogue& ep = PointEpilogue(), long long cell_begin = 0, long long cell_end = -1);
 void general_diagonal(const GeneralGeom& g, const FE1D& fe, void* out, bool invert, cudaStream_t s);
 void general_rhs(const GeneralGeom& g, const FE1D& fe, const double* fq, const double* gq, const double* hq,
                  double* b, cudaStream_t s);

@@ -67,11 +67,92 @@ exg_op::exg_op(const MeshInfo& m, int deg, double ip_factor, int prec)
   }
 }
 
-void exg_op::apply(const void* src, void* dst, int n_rhs, cudaStream_t s, const exg::PointEpilogue& ep) const {
-  if (cartesian)
-    cart_apply(cart, precision, src, dst, n_rhs, cpb, s, ep);
-  else
-    general_apply(*geo, fe, src, dst, n_rhs, s, ep);
+void exg_op::apply(const void* src, void* dst, int n_rhs, cudaStream_t s, const exg::PointEpilogue& ep,
+                   long long cell_begin, long long cell_end) const {
+  const long long nc = mesh.n_cells();
+  if (cell_end < 0) cell_end = nc;
+  EXG_CHECK(cell_begin >= 0 && cell_begin < cell_end && cell_end <= nc, EXG_ERR_INVALID, "bad cell range");
+  if (cartesian) {
+    if (cell_begin == 0 && cell_end == nc) {
+      cart_apply(cart, precision, src, dst, n_rhs, cpb, s, ep);
+    } else {
+      CartHost part = cart;
+      part.mesh.cell_begin = cell_begin;
+      part.mesh.cell_end = cell_end;
+      cart_apply(part, precision, src, dst, n_rhs, cpb, s, ep);
+    }
+  } else {
+    general_apply(*geo, fe, src, dst, n_rhs, s, ep, cell_begin, cell_end);
+  }
+}
+
+HostPipe::~HostPipe() {
+  for (cudaEvent_t e : loaded) cudaEventDestroy(e);
+  for (cudaEvent_t e : done) cudaEventDestroy(e);
+  for (cudaEvent_t e : {start, end})
+    if (e) cudaEventDestroy(e);
+  for (cudaStream_t t : {in, comp, out})
+    if (t) cudaStreamDestroy(t);
+  for (double* p : {src, dst})
+    if (p) cudaFree(p);
+}
+
+// The mesh is cut into K slabs of z-planes (contiguous cell and DoF ranges).  Slab j is copied in
+// on one stream, applied on a second once the slabs it touches through faces are resident, and
+// copied out on a third, so the host-to-device copy of slab j+1, the apply of slab j and the copy
+// back of slab j-1 overlap.  With periodicity in z, slab 0 needs slab K-1 and is applied last.
+void exg_op::apply_host(const double* src_host, double* dst_host, int n_slabs, cudaStream_t s) {
+  EXG_CHECK(precision != EXG_PREC_F32, EXG_ERR_INVALID, "host apply needs an FP64-storage operator");
+  const int Nz = mesh.N[2];
+  const int K = std::max(1, std::min(n_slabs, Nz));
+  const long long plane_dofs = (long long)mesh.N[0] * mesh.N[1] * n * n * n;
+  const long long plane_cells = (long long)mesh.N[0] * mesh.N[1];
+  if (!pipe) {
+    pipe.reset(new HostPipe());
+    pipe->src = (double*)dalloc(n_dofs() * 8);
+    pipe->dst = (double*)dalloc(n_dofs() * 8);
+    EXG_CUDA(cudaStreamCreateWithFlags(&pipe->in, cudaStreamNonBlocking));
+    EXG_CUDA(cudaStreamCreateWithFlags(&pipe->comp, cudaStreamNonBlocking));
+    EXG_CUDA(cudaStreamCreateWithFlags(&pipe->out, cudaStreamNonBlocking));
+    EXG_CUDA(cudaEventCreateWithFlags(&pipe->start, cudaEventDisableTiming));
+    EXG_CUDA(cudaEventCreateWithFlags(&pipe->end, cudaEventDisableTiming));
+  }
+  HostPipe& P = *pipe;
+  while ((int)P.loaded.size() < K) {
+    cudaEvent_t a, b;
+    EXG_CUDA(cudaEventCreateWithFlags(&a, cudaEventDisableTiming));
+    EXG_CUDA(cudaEventCreateWithFlags(&b, cudaEventDisableTiming));
+    P.loaded.push_back(a);
+    P.done.push_back(b);
+  }
+  auto zb = [&](int j) { return (int)((long long)Nz * j / K); };  // first plane of slab j
+  EXG_CUDA(cudaEventRecord(P.start, s));
+  EXG_CUDA(cudaStreamWaitEvent(P.in, P.start, 0));
+  EXG_CUDA(cudaStreamWaitEvent(P.out, P.start, 0));
+  for (int j = 0; j < K; ++j) {
+    const long long off = zb(j) * plane_dofs, len = (long long)(zb(j + 1) - zb(j)) * plane_dofs;
+    EXG_CUDA(cudaMemcpyAsync(P.src + off, src_host + off, len * 8, cudaMemcpyHostToDevice, P.in));
+    EXG_CUDA(cudaEventRecord(P.loaded[j], P.in));
+  }
+  const bool zper = mesh.d.periodic[2] != 0 && K > 1;
+  std::vector<int> order;
+  for (int j = zper ? 1 : 0; j < K; ++j) order.push_back(j);
+  if (zper) order.push_back(0);
+  for (int j : order) {
+    const int need = (zper && j == 0) ? K - 1 : std::min(j + 1, K - 1);
+    EXG_CUDA(cudaStreamWaitEvent(P.comp, P.loaded[need], 0));
+    apply(P.src, P.dst, 1, P.comp, PointEpilogue(), zb(j) * plane_cells, zb(j + 1) * plane_cells);
+    EXG_CUDA(cudaEventRecord(P.done[j], P.comp));
+    const long long off = zb(j) * plane_dofs, len = (long long)(zb(j + 1) - zb(j)) * plane_dofs;
+    EXG_CUDA(cudaStreamWaitEvent(P.out, P.done[j], 0));
+    EXG_CUDA(cudaMemcpyAsync(dst_host + off, P.dst + off, len * 8, cudaMemcpyDeviceToHost, P.out));
+  }
+  // the caller's stream continues after the last copy back (and after the apply stream, so the
+  // next call's copies into the device buffers follow this call's reads)
+  EXG_CUDA(cudaEventRecord(P.end, P.out));
+  EXG_CUDA(cudaStreamWaitEvent(s, P.end, 0));
+  EXG_CUDA(cudaEventRecord(P.end, P.comp));
+  EXG_CUDA(cudaStreamWaitEvent(s, P.end, 0));
 }
 
 void exg_op::diagonal(void* d, bool invert, cudaStream_t s) const {

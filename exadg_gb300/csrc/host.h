@@ -25,6 +25,16 @@ struct CGWorkspace {
   Reduction red;
   ~CGWorkspace();
 };
+
+// device buffers, streams and events of the host-vector apply (exg_sipg_apply_host_f64)
+struct HostPipe {
+  double* src = nullptr;
+  double* dst = nullptr;
+  cudaStream_t in = nullptr, comp = nullptr, out = nullptr;
+  std::vector<cudaEvent_t> loaded, done;
+  cudaEvent_t start = nullptr, end = nullptr;
+  ~HostPipe();
+};
 }  // namespace exg
 
 // SIPG Laplace operator (Poisson::LaplaceOperator)
@@ -42,8 +52,12 @@ struct exg_op {
 
   exg_op(const exg::MeshInfo& m, int degree, double ip, int precision);
   long long n_dofs() const { return mesh.n_cells() * n * n * n; }
+  // dst = A src on the cells [cell_begin, cell_end) (cell_end < 0: all cells)
   void apply(const void* src, void* dst, int n_rhs, cudaStream_t s,
-             const exg::PointEpilogue& ep = exg::PointEpilogue()) const;
+             const exg::PointEpilogue& ep = exg::PointEpilogue(), long long cell_begin = 0,
+             long long cell_end = -1) const;
+  // dst_host = A src_host for FP64 host vectors, copies pipelined against the apply by z-slabs
+  void apply_host(const double* src_host, double* dst_host, int n_slabs, cudaStream_t s);
   void diagonal(void* d, bool invert, cudaStream_t s) const;
   void quadrature_points(double* cx, double* fx, long long* ncp, long long* nfp, cudaStream_t s);
   void rhs(const double* f, const double* g, const double* h, double* b, cudaStream_t s);
@@ -51,6 +65,7 @@ struct exg_op {
   int tune(int n_rhs, cudaStream_t s, std::vector<std::pair<int, float>>* timings);
   exg::CGWorkspace& workspace();
   std::unique_ptr<exg::CGWorkspace> ws;
+  std::unique_ptr<exg::HostPipe> pipe;
 };
 
 namespace exg {

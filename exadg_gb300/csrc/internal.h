@@ -66,6 +66,7 @@ struct CartMesh {
   int bc[6];  // 0 Dirichlet, 1 Neumann
   long long n_cells;
   long long n_dofs;
+  long long cell_begin, cell_end;  // cells written by a launch (row kernels): [cell_begin, cell_end)
 };
 
 // penalty data for Cartesian meshes: tau_c = sum_e (wL_e + wR_e) / h_e

@@ -288,12 +288,12 @@ __global__ void __launch_bounds__(CPB* N* N) cart_apply_kernel(const T* __restri
   C* wy = wx + CPB * N3;
   C* wz = wy + CPB * N3;
 
-  const long long c0 = (long long)blockIdx.x * CPB;
+  const long long c0 = m.cell_begin + (long long)blockIdx.x * CPB;
   const T* s = src + (long long)blockIdx.y * m.n_dofs;
   T* o = dst + (long long)blockIdx.y * m.n_dofs;
   const int tid = threadIdx.x;
   const long long base = c0 * N3;
-  const long long ncell_here = min((long long)CPB, m.n_cells - c0);
+  const long long ncell_here = min((long long)CPB, m.cell_end - c0);
   const int nd = (int)(ncell_here * N3);
 
   for (int i = tid; i < CPB * N3; i += NT) su[i] = i < nd ? load_as<C>(s + base + i) : C(0);
@@ -302,7 +302,7 @@ __global__ void __launch_bounds__(CPB* N* N) cart_apply_kernel(const T* __restri
     long long c = c0 + lc;
     int nb = -1, kind = 2;
     C at = C(0);
-    if (c < m.n_cells) face_info<N, C>(m, P, (int)c, f, nb, kind, at);
+    if (c < m.cell_end) face_info<N, C>(m, P, (int)c, f, nb, kind, at);
     snb[t] = nb;
     skind[t] = kind;
     stau[t] = at;
@@ -660,7 +660,7 @@ static void launch_apply(const CartHost& h, const void* src, void* dst, int n_rh
     EXG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_set = true;
   }
-  long long blocks = (h.mesh.n_cells + CPB - 1) / CPB;
+  long long blocks = (h.mesh.cell_end - h.mesh.cell_begin + CPB - 1) / CPB;
   EXG_CHECK(blocks < (1LL << 31), EXG_ERR_INVALID, "mesh too large");
   EXG_CHECK(n_rhs >= 1 && n_rhs <= 65535, EXG_ERR_INVALID, "n_rhs out of range");
   dim3 grid((unsigned)blocks, (unsigned)n_rhs);
@@ -706,6 +706,8 @@ template <int N, class T, class C>
 static void apply_n(const CartHost& h, const void* src, void* dst, int n_rhs, int cpb, cudaStream_t s,
                     const PointEpilogue& ep) {
   using BC = BrickChoice<N>;
+  // bricks cover the whole mesh; a launch over a cell range uses the row kernel
+  if (cpb < 0 && (h.mesh.cell_begin != 0 || h.mesh.cell_end != h.mesh.n_cells)) cpb = CpbChoice<N>::b;
   if (cpb == -1)
     launch_brick<N, BC::ax, BC::ay, BC::az, T, C>(h, src, dst, n_rhs, s, ep);
   else if (cpb == -2)

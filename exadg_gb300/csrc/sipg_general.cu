@@ -346,8 +346,9 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
                                                               const __grid_constant__ GenCoef<N, C> P,
                                                               const C* __restrict__ cellG, const C* __restrict__ face,
                                                               const C* __restrict__ ftau,
-                                                              const long long* __restrict__ fnb, long long n_cells,
-                                                              long long n_dofs, const PointEpilogue ep) {
+                                                              const long long* __restrict__ fnb, long long cell_begin,
+                                                              long long n_cells, long long n_dofs,
+                                                              const PointEpilogue ep) {
   constexpr int N2 = N * N, N3 = N2 * N, NT = CPB * N2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* su = reinterpret_cast<C*>(smem_raw);
@@ -365,7 +366,7 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
     sD[i] = P.D[i];
   }
 
-  const long long c0 = (long long)blockIdx.x * CPB;
+  const long long c0 = cell_begin + (long long)blockIdx.x * CPB;  // cells [cell_begin, n_cells)
   const T* s = src + (long long)blockIdx.y * n_dofs;
   T* o = dst + (long long)blockIdx.y * n_dofs;
   const int tid = threadIdx.x;
@@ -675,7 +676,7 @@ constexpr int gen_cpb() {
 
 template <int N, class T, class C>
 static void gen_apply_n(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s,
-                        const PointEpilogue& ep) {
+                        const PointEpilogue& ep, long long cb, long long ce) {
   constexpr int CPB = gen_cpb<N>(), N3 = N * N * N, N2 = N * N;
   GenCoef<N, C> P = gen_coef<N, C>(fe);
   size_t smem = (5 * (size_t)CPB * N3 + (size_t)CPB * 16 * N2) * sizeof(C);
@@ -685,39 +686,41 @@ static void gen_apply_n(const GeneralGeom& g, const FE1D& fe, const void* src, v
     EXG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     attr_set = true;
   }
-  long long blocks = (g.n_cells + CPB - 1) / CPB;
+  long long blocks = (ce - cb + CPB - 1) / CPB;
   dim3 grid((unsigned)blocks, (unsigned)n_rhs);
   kern<<<grid, CPB * N2, smem, s>>>((const T*)src, (T*)dst, P, (const C*)g.cellG, (const C*)g.face, (const C*)g.ftau,
-                                    g.fnb, g.n_cells, g.n_cells * N3, ep);
+                                    g.fnb, cb, ce, g.n_cells * N3, ep);
   EXG_CUDA(cudaGetLastError());
 }
 
 template <class T, class C>
 static void gen_apply_t(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s,
-                        const PointEpilogue& ep) {
+                        const PointEpilogue& ep, long long cb, long long ce) {
   switch (fe.n) {
-    case 2: gen_apply_n<2, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
-    case 3: gen_apply_n<3, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
-    case 4: gen_apply_n<4, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
-    case 5: gen_apply_n<5, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
-    case 6: gen_apply_n<6, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
-    case 7: gen_apply_n<7, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
-    case 8: gen_apply_n<8, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
-    case 9: gen_apply_n<9, T, C>(g, fe, src, dst, n_rhs, s, ep); break;
+    case 2: gen_apply_n<2, T, C>(g, fe, src, dst, n_rhs, s, ep, cb, ce); break;
+    case 3: gen_apply_n<3, T, C>(g, fe, src, dst, n_rhs, s, ep, cb, ce); break;
+    case 4: gen_apply_n<4, T, C>(g, fe, src, dst, n_rhs, s, ep, cb, ce); break;
+    case 5: gen_apply_n<5, T, C>(g, fe, src, dst, n_rhs, s, ep, cb, ce); break;
+    case 6: gen_apply_n<6, T, C>(g, fe, src, dst, n_rhs, s, ep, cb, ce); break;
+    case 7: gen_apply_n<7, T, C>(g, fe, src, dst, n_rhs, s, ep, cb, ce); break;
+    case 8: gen_apply_n<8, T, C>(g, fe, src, dst, n_rhs, s, ep, cb, ce); break;
+    case 9: gen_apply_n<9, T, C>(g, fe, src, dst, n_rhs, s, ep, cb, ce); break;
     default: throw Error{EXG_ERR_UNSUPPORTED, "degree must be 1..8"};
   }
 }
 
 void general_apply(const GeneralGeom& g, const FE1D& fe, const void* src, void* dst, int n_rhs, cudaStream_t s,
-                   const PointEpilogue& ep) {
+                   const PointEpilogue& ep, long long cell_begin, long long cell_end) {
+  if (cell_end < 0) cell_end = g.n_cells;
+  EXG_CHECK(cell_begin >= 0 && cell_begin < cell_end && cell_end <= g.n_cells, EXG_ERR_INVALID, "bad cell range");
   EXG_CHECK(n_rhs >= 1 && n_rhs <= 65535, EXG_ERR_INVALID, "n_rhs out of range");
   EXG_CHECK(ep.mode < 0 || n_rhs == 1, EXG_ERR_INVALID, "fused point update needs a single right-hand side");
   if (g.precision == EXG_PREC_F32)
-    gen_apply_t<float, float>(g, fe, src, dst, n_rhs, s, ep);
+    gen_apply_t<float, float>(g, fe, src, dst, n_rhs, s, ep, cell_begin, cell_end);
   else if (g.precision == EXG_PREC_F64E)
-    gen_apply_t<double, df64>(g, fe, src, dst, n_rhs, s, ep);
+    gen_apply_t<double, df64>(g, fe, src, dst, n_rhs, s, ep, cell_begin, cell_end);
   else
-    gen_apply_t<double, double>(g, fe, src, dst, n_rhs, s, ep);
+    gen_apply_t<double, double>(g, fe, src, dst, n_rhs, s, ep, cell_begin, cell_end);
 }
 
 // ------------------------------------------------------------------------------------------------

@@ -76,6 +76,15 @@ exg_status exg_sipg_info(const exg_op* op, int* degree, int* precision, int* car
  * EXG_PREC_F32 operators. */
 exg_status exg_sipg_apply_f64(exg_op* op, const double* src, double* dst, int n_rhs, void* stream);
 exg_status exg_sipg_apply_f32(exg_op* op, const float* src, float* dst, int n_rhs, void* stream);
+/* dst = A src for FP64 HOST vectors (the vectors ExaDG holds): the library copies in, applies and
+ * copies back, cutting the mesh into n_slabs slabs of z-planes so that the copies of one slab
+ * overlap the apply of its neighbour (three internal streams, ordered after and before `stream`).
+ * Returns once the work is queued; the result is in dst_host when `stream` has completed.  Pinned
+ * host memory (cudaHostAlloc / cudaHostRegister) is needed for the overlap.  Overlapping calls on
+ * the same operator share its device buffers and race.  FP64-storage operators
+ * (OperatorBase::vmult on host vectors, operators/operator_base.cpp:156-168). */
+exg_status exg_sipg_apply_host_f64(exg_op* op, const double* src_host, double* dst_host, int n_slabs,
+                                   void* stream);
 /* r = b - A x in one kernel (the residual step of the V-cycle and of its residual check,
  * multigrid/multigrid_algorithm.h:155-160, 215-216); r must not alias x.  FP64 storage operators. */
 exg_status exg_sipg_residual_f64(exg_op* op, const double* b, const double* x, double* r, void* stream);

@@ -512,7 +512,7 @@ def run_learned(args):
     rhs, dt = LG.tgv_rhs_sequence(steps, n_cells=32, degree=2)
     gen_s = time.perf_counter() - t0
     res = {}
-    for mode in ("extrapolation", "untrained", "learned"):
+    for mode in ("extrapolation", "extrapolation3", "untrained", "learned"):
         seq = LG.PressureSequence(n_cells=32, degree=2, mode=mode, train_every=20, epochs=args.learned_epochs)
         seq.diagnostics = args.learned_diagnostics
         for b in rhs:
@@ -527,8 +527,8 @@ def run_learned(args):
             "mean_guess_s_second_half": statistics.mean(r["guess_s"] for r in tail),
             "mean_total_s_second_half": statistics.mean(r["solve_s"] + r["guess_s"] for r in tail),
             "mean_r0_rel_second_half": statistics.mean(r["r0_rel"] for r in tail),
-            "sources": {s_: sum(1 for r in log if r["source"] == s_) for s_ in ("zero", "previous", "extrapolation",
-                                                                              "learned", "fallback")},
+            "sources": {s_: sum(1 for r in log if r["source"] == s_)
+                        for s_ in ("zero", "previous", "extrapolation", "extrapolation3", "learned", "fallback")},
             "mean_r_ext_rel_second_half": statistics.mean(r.get("r_ext_rel", r["r0_rel"]) for r in tail),
             "train_s_total": sum(r.get("train_s", 0.0) for r in log),
             "iterations": [r["iterations"] for r in log],
@@ -542,7 +542,7 @@ def run_learned(args):
             res[mode]["loss_last_round"] = last[-1]["loss_last"]
         del seq
         torch.cuda.synchronize()
-    e, l, u = res["extrapolation"], res["learned"], res["untrained"]
+    e, l, u, e3 = res["extrapolation"], res["learned"], res["untrained"], res["extrapolation3"]
     line = {"metric": "PPE CG iterations per solve, learned guess vs BDF2 extrapolation (TGV 32^3, k_p=2)",
             "value": l["mean_iterations_second_half"], "unit": "iterations", "higher_is_better": False,
             "mode": "learned", "data": "synthetic: TGV Re=1600 pressure sources from a pseudo-spectral integrator",
@@ -550,6 +550,8 @@ def run_learned(args):
             "iteration_gain_second_half": e["mean_iterations_second_half"] - l["mean_iterations_second_half"],
             "iteration_gain_trained_vs_untrained": u["mean_iterations_second_half"] - l["mean_iterations_second_half"],
             "time_gain_second_half": e["mean_total_s_second_half"] / l["mean_total_s_second_half"],
+            "iteration_gain_vs_third_order_ls": e3["mean_iterations_second_half"] - l["mean_iterations_second_half"],
+            "time_gain_vs_third_order_ls": e3["mean_total_s_second_half"] / l["mean_total_s_second_half"],
             "results": res}
     print(json.dumps(line))
     return 0

@@ -173,8 +173,8 @@ def load_library(path=LIB_PATH):
         "exg_dg_pack": [P, P, I, I, LL, P, P],
         "exg_dg_unpack_add": [P, P, D, I, LL, P, P],
         "exg_dg_pack_diff": [P, P, D, I, LL, P, P],
-        "exg_dg_features": [P, P, P, P, I, LL, P, P, P],
-        "exg_dg_ls_step": [P, P, P, P, LL, P, P, P],
+        "exg_dg_features": [P, P, P, P, I, LL, D, P, P, P],
+        "exg_dg_ls_step": [P, P, P, P, P, P, LL, P, P, P],
     }
     for name, args in sig.items():
         f = getattr(L, name)

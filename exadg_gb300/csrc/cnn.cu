@@ -257,35 +257,43 @@ __global__ void pack_diff_kernel(const double* __restrict__ a, const double* __r
 // quantity).  Calls that overlap on the GPU share the partials array and race.
 // ---------------------------------------------------------------------------------------------------
 static constexpr int RED_NB = 608;  // 4 blocks per SM
-__device__ double g_dg_partials[4 * RED_NB];
+__device__ double g_dg_partials[6 * RED_NB];
 
 __device__ __forceinline__ double warp_sum_d(double v) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
   return v;
 }
 
-// partials[j][block] = sum over the block's entries of f_j^2 (NF = 4: features) or of the products
-// (NF = 3: r.Ae, Ae.Ae, r.r)
-template <int NF>
+// partials[j][block] = the block's part of sum_i q_j(i):
+//   KIND 0 (features, a = p0, b = p1, c = p2, d = r): p0^2, d1^2, d2^2, r^2
+//   KIND 1 (least squares, a = r, b = Ae, c = Af or null): r.Ae, Ae.Ae, r.r, r.Af, Af.Af, Ae.Af
+template <int KIND>
 __global__ void __launch_bounds__(256) dg_partials_kernel(const double* __restrict__ a, const double* __restrict__ b,
                                                           const double* __restrict__ c, const double* __restrict__ d,
                                                           long long n) {
+  constexpr int NF = KIND == 0 ? 4 : 6;
   double acc[NF];
 #pragma unroll
   for (int j = 0; j < NF; ++j) acc[j] = 0.0;
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
-    if constexpr (NF == 4) {  // a = p0, b = p1, c = p2, d = r
+    if constexpr (KIND == 0) {
       const double p0 = a[i], p1 = b[i], p2 = c[i], rr = d[i];
       const double d1 = p0 - p1, d2 = p0 - 2.0 * p1 + p2;
       acc[0] += p0 * p0;
       acc[1] += d1 * d1;
       acc[2] += d2 * d2;
       acc[3] += rr * rr;
-    } else {  // a = r, b = Ae
+    } else {
       const double r = a[i], ae = b[i];
       acc[0] += r * ae;
       acc[1] += ae * ae;
       acc[2] += r * r;
+      if (c) {
+        const double af = c[i];
+        acc[3] += r * af;
+        acc[4] += af * af;
+        acc[5] += ae * af;
+      }
     }
   }
   __shared__ double sh[NF][8];
@@ -303,10 +311,11 @@ __global__ void __launch_bounds__(256) dg_partials_kernel(const double* __restri
   }
 }
 
-// one warp per quantity: out[j] = sum of partials[j][:] (then mode 0: rms = sqrt(sum / n);
-// mode 1: out = {r.Ae, Ae.Ae, r.r, step}, step = max(r.Ae / Ae.Ae, 0), 0 when not finite)
-__global__ void dg_finalize_kernel(int nq, int mode, long long n, double* __restrict__ out) {
-  __shared__ double tot[4];
+// one warp per quantity sums the partials in index order, then
+//   mode 0: out[0..3] = RMS of the features; out[2] = diff_scale if diff_scale > 0
+//   mode 1: least-squares step lengths along e (and f), see exg_dg_ls_step
+__global__ void dg_finalize_kernel(int nq, int mode, long long n, double diff_scale, double* __restrict__ out) {
+  __shared__ double tot[6];
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
   if (w < nq) {
     double v = 0.0;
@@ -315,18 +324,35 @@ __global__ void dg_finalize_kernel(int nq, int mode, long long n, double* __rest
     if (l == 0) tot[w] = v;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    if (mode == 0) {
-      for (int j = 0; j < nq; ++j) out[j] = fmax(sqrt(tot[j] / (double)n), 1e-300);
-    } else {
-      double c = tot[1] > 0.0 ? tot[0] / tot[1] : 0.0;
-      if (!(c > 0.0) || !isfinite(c)) c = 0.0;
-      out[0] = tot[0];
-      out[1] = tot[1];
-      out[2] = tot[2];
-      out[3] = c;
+  if (threadIdx.x != 0) return;
+  if (mode == 0) {
+    for (int j = 0; j < 4; ++j) out[j] = fmax(sqrt(tot[j] / (double)n), 1e-300);
+    if (diff_scale > 0.0) out[2] = diff_scale;
+    return;
+  }
+  // minimise |r - ce Ae - cf Af|: normal equations [[Ae.Ae, Ae.Af], [Ae.Af, Af.Af]] (ce, cf) = (r.Ae, r.Af)
+  const double rae = tot[0], aa = tot[1], rr = tot[2];
+  double ce = aa > 0.0 ? rae / aa : 0.0, cf = 0.0;
+  if (nq == 6) {
+    const double raf = tot[3], ff = tot[4], af = tot[5];
+    const double det = aa * ff - af * af;
+    if (det > 1e-12 * aa * ff && aa > 0.0 && ff > 0.0) {
+      ce = (rae * ff - raf * af) / det;
+      cf = (raf * aa - rae * af) / det;
+    } else if (ff > 0.0 && raf * raf / ff > rae * rae / fmax(aa, 1e-300)) {
+      ce = 0.0;  // (nearly) parallel directions: the better single one
+      cf = raf / ff;
     }
   }
+  if (!isfinite(ce) || !isfinite(cf)) ce = cf = 0.0;
+  double red = ce * rae + cf * (nq == 6 ? tot[3] : 0.0);  // |r|^2 - |r - ce Ae - cf Af|^2
+  if (!(red > 1e-14 * rr)) ce = cf = 0.0;  // no decrease beyond rounding: plain base (fallback)
+  out[0] = rae;
+  out[1] = aa;
+  out[2] = rr;
+  out[3] = ce;
+  out[4] = cf;
+  out[5] = ce == 0.0 && cf == 0.0 ? 0.0 : red;
 }
 
 // x[j*npc + i][c] = f_j[c*npc + i] / rms_j with f = (p0, p0 - p1, p0 - 2 p1 + p2, r)
@@ -352,12 +378,13 @@ __global__ void dg_features_pack_kernel(const double* __restrict__ p0, const dou
   x[g] = (float)(v / rms[j]);
 }
 
-// x = base + stats[3] e
+// x = base + stats[3] e + stats[4] f (f optional)
 __global__ void dg_step_kernel(const double* __restrict__ base, const double* __restrict__ e,
-                               const double* __restrict__ stats, long long n, double* __restrict__ x) {
-  const double c = stats[3];
+                               const double* __restrict__ f, const double* __restrict__ stats, long long n,
+                               double* __restrict__ x) {
+  const double ce = stats[3], cf = stats[4];
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    x[i] = base[i] + c * e[i];
+    x[i] = base[i] + ce * e[i] + (f ? cf * f[i] : 0.0);
 }
 
 // ---------------------------------------------------------------------------------------------------
@@ -651,14 +678,15 @@ exg_status exg_dg_pack_diff(const double* a, const double* b, double inv_scale, 
 }
 
 exg_status exg_dg_features(const double* p0, const double* p1, const double* p2, const double* r,
-                           int dofs_per_cell, long long n_cells, float* x, double* rms, void* stream) {
+                           int dofs_per_cell, long long n_cells, double diff_scale, float* x, double* rms,
+                           void* stream) {
   CNN_BEGIN
   EXG_CHECK(p0 && p1 && p2 && r && x && rms, EXG_ERR_INVALID, "null argument");
   EXG_CHECK(dofs_per_cell >= 1 && n_cells >= 1, EXG_ERR_INVALID, "empty vectors");
   cudaStream_t s = (cudaStream_t)stream;
   const long long n = n_cells * dofs_per_cell;
-  dg_partials_kernel<4><<<RED_NB, 256, 0, s>>>(p0, p1, p2, r, n);
-  dg_finalize_kernel<<<1, 128, 0, s>>>(4, 0, n, rms);
+  dg_partials_kernel<0><<<RED_NB, 256, 0, s>>>(p0, p1, p2, r, n);
+  dg_finalize_kernel<<<1, 128, 0, s>>>(4, 0, n, diff_scale, rms);
   const long long tot = 4 * n;
   dg_features_pack_kernel<<<(unsigned)((tot + 255) / 256), 256, 0, s>>>(p0, p1, p2, r, rms, dofs_per_cell, n_cells,
                                                                         x);
@@ -666,15 +694,16 @@ exg_status exg_dg_features(const double* p0, const double* p1, const double* p2,
   CNN_END
 }
 
-exg_status exg_dg_ls_step(const double* r, const double* Ae, const double* e, const double* base, long long n,
-                          double* x, double* stats, void* stream) {
+exg_status exg_dg_ls_step(const double* r, const double* Ae, const double* e, const double* Af, const double* f,
+                          const double* base, long long n, double* x, double* stats, void* stream) {
   CNN_BEGIN
   EXG_CHECK(r && Ae && e && base && x && stats, EXG_ERR_INVALID, "null argument");
+  EXG_CHECK((Af == nullptr) == (f == nullptr), EXG_ERR_INVALID, "give both f and A f, or neither");
   EXG_CHECK(n >= 1, EXG_ERR_INVALID, "empty vectors");
   cudaStream_t s = (cudaStream_t)stream;
-  dg_partials_kernel<3><<<RED_NB, 256, 0, s>>>(r, Ae, nullptr, nullptr, n);
-  dg_finalize_kernel<<<1, 128, 0, s>>>(3, 1, n, stats);
-  dg_step_kernel<<<RED_NB * 2, 256, 0, s>>>(base, e, stats, n, x);
+  dg_partials_kernel<1><<<RED_NB, 256, 0, s>>>(r, Ae, Af, nullptr, n);
+  dg_finalize_kernel<<<1, 192, 0, s>>>(f ? 6 : 3, 1, n, 0.0, stats);
+  dg_step_kernel<<<RED_NB * 2, 256, 0, s>>>(base, e, f, stats, n, x);
   EXG_CUDA(cudaGetLastError());
   CNN_END
 }

@@ -432,17 +432,23 @@ __device__ __forceinline__ void cta_sum2(R& a, R& b, R* sh) {
   b = sh[65];
 }
 
-// out = A in with one warp per row (A symmetric, so row i is read contiguously; lane-strided
-// partial sums reduced by a fixed shuffle tree: deterministic)
+// out = A in with one thread per row.  The matrix is stored by columns (A[j*n + i] = A_ij, column j
+// being the operator applied to e_j), so the threads of a warp read consecutive addresses
+// (conflict-free in shared memory, coalesced in global memory); four partial sums per thread give
+// independent FMA chains.  The summation order is fixed, so results are deterministic.
 template <class CT>
 __device__ __forceinline__ void coarse_matvec(const CT* A, const CT* in, CT* out, int n) {
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int i = warp; i < n; i += nw) {
-    const CT* Ai = A + (long long)i * n;
-    CT acc = 0;
-    for (int j = lane; j < n; j += 32) acc += Ai[j] * in[j];
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
-    if (lane == 0) out[i] = acc;
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    CT a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+    int j = 0;
+    for (; j + 3 < n; j += 4) {
+      a0 += A[(long long)j * n + i] * in[j];
+      a1 += A[(long long)(j + 1) * n + i] * in[j + 1];
+      a2 += A[(long long)(j + 2) * n + i] * in[j + 2];
+      a3 += A[(long long)(j + 3) * n + i] * in[j + 3];
+    }
+    for (; j < n; ++j) a0 += A[(long long)j * n + i] * in[j];
+    out[i] = (a0 + a1) + (a2 + a3);
   }
   __syncthreads();
 }

@@ -8,12 +8,13 @@ correction to that extrapolation from, per cell, the DG coefficients of the last
 the residual of the extrapolation, b - A p_ext).  It is trained online on the solver's own
 converged pressures every `train_every` steps in the energy norm that CG minimises,
 L = (d - e)^T A (d - e) / d^T A d with d = p - p_ext and e = s y(x) (A (d - e) = r_ext - A e, so the
-gradient costs one operator apply).  At inference the correction is scaled by the one-term
-least-squares coefficient c = <r_ext, A e> / ||A e||^2, so the learned guess p_ext + c e never has a
-larger residual than p_ext (||r_ext - c A e||^2 = ||r_ext||^2 - c <r_ext, A e>); when c is not
-positive the plain extrapolation is used (fallback).  Feature scaling, c and the fallback are
-computed on the device, so building the guess needs no host round trip.  Both seedings run FP64
-CG + FP32 multigrid to the same tolerance, ||r|| <= tol * ||b||.
+gradient costs one operator apply).  At inference the guess is p_ext + c e + c3 d2, d2 = p^n -
+2 p^{n-1} + p^{n-2}, with (c, c3) minimising the residual (two operator applies, a 2x2 system): it
+never has a larger residual than p_ext nor than the least-squares third-order extrapolation; when
+neither direction reduces the residual the plain extrapolation is used (fallback).  Mode
+"extrapolation3" is that third-order baseline without a network.  Feature scaling, the step
+lengths and the fallback are computed on the device, so building the guess needs no host round
+trip.  All seedings run FP64 CG + FP32 multigrid to the same tolerance, ||r|| <= tol * ||b||.
 """
 import time
 
@@ -29,7 +30,7 @@ def _rms(t):
 
 class PressureSequence:
     def __init__(self, n_cells=32, degree=2, length=6.283185307179586, mode="learned", train_every=20,
-                 epochs=40, lr=1e-3, buffer=20, hidden=32, seed=1, tol=1e-10, outer_precision=E.PREC_F64E):
+                 epochs=40, lr=1e-4, buffer=20, hidden=32, seed=1, tol=1e-10, outer_precision=E.PREC_F64E):
         import torch
 
         self.torch = torch
@@ -58,6 +59,13 @@ class PressureSequence:
             w4 = self.cnn.params[off:off + self.dpc * 4 * self.dpc].view(self.dpc, 4 * self.dpc)
             w4.zero_()
             w4[:, 2 * self.dpc:3 * self.dpc] += torch.eye(self.dpc, device="cuda")
+            # the last convolution (W3, b3) starts at zero, so the untrained network is exactly the
+            # third-order term and training learns a correction to it
+            shapes = self.cnn.layer_shapes()
+            o3 = sum(int(torch.tensor(sh).prod()) for _, sh in shapes[:4])
+            n3 = sum(int(torch.tensor(sh).prod()) for _, sh in shapes[4:6])
+            self.cnn.params[o3:o3 + n3].zero_()
+            self.w4_slice = (off, off + self.dpc * 4 * self.dpc)
         self.trained = mode == "untrained"
         self.delta_scale = None
         self.x = torch.empty((4 * self.dpc, self.nc), dtype=torch.float32, device="cuda")
@@ -67,6 +75,7 @@ class PressureSequence:
         self.zero = torch.zeros(n, dtype=torch.float64, device="cuda")
         self.e = torch.empty(n, dtype=torch.float64, device="cuda")
         self.Ae = torch.empty(n, dtype=torch.float64, device="cuda")
+        self.Af = torch.empty(n, dtype=torch.float64, device="cuda")
         self.rms = torch.empty(4, dtype=torch.float64, device="cuda")
         self.diagnostics = False
 
@@ -79,14 +88,23 @@ class PressureSequence:
         return self.torch.lerp(self.hist[-2], self.hist[-1], 2.0)
 
     def _features(self, b, p_ext):
-        """Network input from (p^n, p^n - p^{n-1}, p^n - 2 p^{n-1} + p^{n-2}, b - A p_ext), each scaled
-        by its RMS on the device; returns r_ext = b - A p_ext.  No host round trip."""
+        """Network input from (p^n, p^n - p^{n-1}, p^n - 2 p^{n-1} + p^{n-2}, b - A p_ext) on the device;
+        each is scaled by its RMS except the second difference, which is scaled by the running RMS
+        of the corrections (the scale of the output), so that the linear skip reproduces the
+        third-order term exactly.  Returns r_ext = b - A p_ext.  No host round trip."""
         r_ext = self.torch.empty_like(p_ext)
         self.op.residual(r_ext, b, p_ext)
         E._check(E._lib.exg_dg_features(E._ptr(self.hist[-1]), E._ptr(self.hist[-2]), E._ptr(self.hist[-3]),
-                                        E._ptr(r_ext), self.dpc, self.nc, E._ptr(self.x), E._ptr(self.rms),
-                                        E._stream()))
+                                        E._ptr(r_ext), self.dpc, self.nc, self.delta_scale or 0.0, E._ptr(self.x),
+                                        E._ptr(self.rms), E._stream()))
         return r_ext
+
+    def _second_difference(self):
+        """p^n - 2 p^{n-1} + p^{n-2}: the third-order extrapolation adds it to p_ext."""
+        d2 = self.hist[-1] - self.hist[-2]
+        d2 -= self.hist[-2]
+        d2 += self.hist[-3]
+        return d2
 
     def initial_guess(self, b):
         """Returns (guess, info).  The learned branch runs without a host round trip: the step length
@@ -101,6 +119,18 @@ class PressureSequence:
             return self.hist[-1].clone(), info
         p_ext = self._extrapolation()
         info["source"] = "extrapolation"
+        x = torch.empty_like(p_ext)
+        stats = torch.empty(6, dtype=torch.float64, device="cuda")
+        if self.mode == "extrapolation3" and len(self.hist) >= 3:
+            # baseline without a network: p_ext + c (p^n - 2 p^{n-1} + p^{n-2}), c by least squares
+            r_ext = self._residual(b, p_ext)
+            d2 = self._second_difference()
+            self.op.vmult(self.Ae, d2)
+            E._check(E._lib.exg_dg_ls_step(E._ptr(r_ext), E._ptr(self.Ae), E._ptr(d2), None, None, E._ptr(p_ext),
+                                           self.op.n_dofs, E._ptr(x), E._ptr(stats), E._stream()))
+            info["stats"] = stats
+            info["kind"] = "extrapolation3"
+            return x, info
         if self.cnn is None or len(self.hist) < 3 or not self.trained or self.delta_scale is None:
             return p_ext, info
         r_ext = self._features(b, p_ext)
@@ -108,11 +138,13 @@ class PressureSequence:
         E._check(E._lib.exg_dg_unpack_add(E._ptr(y), E._ptr(self.zero), self.delta_scale, self.dpc, self.nc,
                                           E._ptr(self.e), E._stream()))
         self.op.vmult(self.Ae, self.e)
-        x = torch.empty_like(p_ext)
-        stats = torch.empty(4, dtype=torch.float64, device="cuda")
-        E._check(E._lib.exg_dg_ls_step(E._ptr(r_ext), E._ptr(self.Ae), E._ptr(self.e), E._ptr(p_ext),
-                                       self.op.n_dofs, E._ptr(x), E._ptr(stats), E._stream()))
+        # least squares over span{e, p^n - 2 p^{n-1} + p^{n-2}}: never worse than either direction
+        d2 = self._second_difference()
+        self.op.vmult(self.Af, d2)
+        E._check(E._lib.exg_dg_ls_step(E._ptr(r_ext), E._ptr(self.Ae), E._ptr(self.e), E._ptr(self.Af), E._ptr(d2),
+                                       E._ptr(p_ext), self.op.n_dofs, E._ptr(x), E._ptr(stats), E._stream()))
         info["stats"] = stats
+        info["kind"] = "learned"
         if self.diagnostics:  # residual of the third-order extrapolation p_ext + (p^n - 2p^{n-1} + p^{n-2})
             d2 = self.hist[-1] - 2 * self.hist[-2] + self.hist[-3]
             info["r_ext3"] = float(torch.linalg.norm(self._residual(b, p_ext + d2)))
@@ -123,11 +155,16 @@ class PressureSequence:
         """Reads the device statistics of a learned guess (after the solve has synchronised)."""
         if "stats" not in info:
             return info
-        rae, aa, rr, c = info.pop("stats").tolist()
-        info["c"] = c
+        rae, aa, rr, ce, cf, red = info.pop("stats").tolist()
+        info["c"] = ce
+        info["c_d2"] = cf
         info["r_ext"] = rr ** 0.5
-        info["r_cnn"] = max(rr - c * rae, 0.0) ** 0.5
-        info["source"] = "learned" if c > 0 else "fallback"
+        info["r_cnn"] = max(rr - red, 0.0) ** 0.5
+        kind = info.pop("kind")
+        if kind == "extrapolation3":
+            info["source"] = "extrapolation3" if ce != 0.0 else "fallback"
+        else:
+            info["source"] = "learned" if (ce != 0.0 or cf != 0.0) else "fallback"
         return info
 
     def _record_sample(self, b, p_new):
@@ -135,10 +172,10 @@ class PressureSequence:
         if self.cnn is None or len(self.hist) < 3:
             return
         p_ext = self._extrapolation()
-        r_ext = self._features(b, p_ext)
         delta = p_new - p_ext
         s = _rms(delta)
         self.delta_scale = s if self.delta_scale is None else 0.8 * self.delta_scale + 0.2 * s
+        r_ext = self._features(b, p_ext)
         self.samples.append((self.x.clone(), r_ext, delta))
         if len(self.samples) > self.buffer_size:
             self.samples.pop(0)
@@ -165,6 +202,9 @@ class PressureSequence:
             E._check(E._lib.exg_dg_pack_diff(E._ptr(zero), E._ptr(res), 2.0 * s / nrm, self.dpc, self.nc,
                                              E._ptr(gy), E._stream()))
             self.cnn.backward(x, gy)
+            # the skip stays the third-order term (Adam's sign-like first steps would only perturb
+            # it); the convolutions learn the correction to it
+            self.cnn.grads[self.w4_slice[0]:self.w4_slice[1]].zero_()
             self.cnn.adam(self.lr)
         self.trained = True
         return losses

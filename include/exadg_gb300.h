@@ -209,18 +209,21 @@ exg_status exg_dg_unpack_add(const float* y, const double* base, double scale, i
                              long long n_cells, double* dst, void* stream);
 /* Network input of the learned guess, all on the device: the four features
  * f = (p0, p0 - p1, p0 - 2 p1 + p2, r) of the DG vectors p0, p1, p2 (newest first) and r, each
- * divided by its root mean square over the DoFs, x[j*dpc + i][c] = f_j[c*dpc + i] / rms[j];
- * rms (4 device doubles) is written too. */
+ * divided by a scale, x[j*dpc + i][c] = f_j[c*dpc + i] / scale[j]; scale[j] is the feature's root
+ * mean square over the DoFs, except for the second difference when diff_scale > 0 (divided by
+ * diff_scale, the scale of the predicted correction, so that the correction can reproduce it
+ * exactly).  The 4 scales are written to `rms` (device doubles). */
 exg_status exg_dg_features(const double* p0, const double* p1, const double* p2, const double* r,
-                           int dofs_per_cell, long long n_cells, float* x, double* rms, void* stream);
-/* Least-squares step along a correction e with Ae = A e, without a host round trip:
- * stats = {r.Ae, Ae.Ae, r.r, c} with c = max(r.Ae / Ae.Ae, 0) (0 if not finite) and x = base + c e.
- * With r = b - A base, the residual of x is r - c Ae, of squared norm r.r - c r.Ae <= r.r: c = 0
- * (plain base) is the fallback when the correction does not reduce the residual.  Calls that
- * overlap on the GPU race (shared reduction array); this and exg_dg_features add no counterpart
- * to the reference. */
-exg_status exg_dg_ls_step(const double* r, const double* Ae, const double* e, const double* base, long long n,
-                          double* x, double* stats, void* stream);
+                           int dofs_per_cell, long long n_cells, double diff_scale, float* x, double* rms,
+                           void* stream);
+/* Least-squares step along one or two corrections without a host round trip: with r = b - A base,
+ * (ce, cf) minimise |r - ce A e - cf A f| (f, Af may be NULL: then cf = 0), x = base + ce e + cf f,
+ * stats = {r.Ae, Ae.Ae, r.r, ce, cf, decrease of |r|^2} (6 device doubles).  The residual of x is
+ * never larger than r; when the corrections do not reduce it, ce = cf = 0 and x = base (the
+ * fallback).  Calls that overlap on the GPU race (shared reduction array); this and
+ * exg_dg_features add no counterpart to the reference. */
+exg_status exg_dg_ls_step(const double* r, const double* Ae, const double* e, const double* Af, const double* f,
+                          const double* base, long long n, double* x, double* stats, void* stream);
 /* t[i][c] = (a[c*dpc + i] - b[c*dpc + i]) * inv_scale */
 exg_status exg_dg_pack_diff(const double* a, const double* b, double inv_scale, int dofs_per_cell,
                             long long n_cells, float* t, void* stream);

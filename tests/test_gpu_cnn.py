@@ -74,33 +74,57 @@ def test_learned_guess_sequence_small():
 
 
 def test_features_and_ls_step_on_device():
-    """exg_dg_features / exg_dg_ls_step against NumPy: feature scaling by RMS, the least-squares step
-    c = max(r.Ae / Ae.Ae, 0) and the fallback (c = 0, x = base) when the correction points uphill."""
+    """exg_dg_features / exg_dg_ls_step against NumPy: feature scaling (own RMS, or the correction
+    scale for the second difference), the one- and two-direction least-squares steps and the fallback
+    (no decrease: x = base)."""
     torch = require_gpu()
     rng = np.random.default_rng(7)
     dpc, nc = 27, 150
     n = dpc * nc
     p0, p1, p2, r = (rng.normal(0, s, n) for s in (1.0, 0.9, 0.8, 1e-3))
     dev = [torch.tensor(v, device="cuda") for v in (p0, p1, p2, r)]
-    x = torch.empty((4 * dpc, nc), dtype=torch.float32, device="cuda")
-    rms = torch.empty(4, dtype=torch.float64, device="cuda")
-    E._check(E._lib.exg_dg_features(*(E._ptr(v) for v in dev), dpc, nc, E._ptr(x), E._ptr(rms), E._stream()))
     feats = [p0, p0 - p1, p0 - 2 * p1 + p2, r]
-    rms_ref = np.array([np.sqrt(np.mean(f * f)) for f in feats])
-    assert np.allclose(rms.cpu().numpy(), rms_ref, rtol=1e-12)
-    x_ref = np.concatenate([(f / s).reshape(nc, dpc).T for f, s in zip(feats, rms_ref)], axis=0)
-    assert np.allclose(x.cpu().numpy(), x_ref, rtol=1e-6, atol=1e-6)
+    for diff_scale in (0.0, 0.37):
+        x = torch.empty((4 * dpc, nc), dtype=torch.float32, device="cuda")
+        rms = torch.empty(4, dtype=torch.float64, device="cuda")
+        E._check(E._lib.exg_dg_features(*(E._ptr(v) for v in dev), dpc, nc, diff_scale, E._ptr(x), E._ptr(rms),
+                                        E._stream()))
+        sc = np.array([np.sqrt(np.mean(f * f)) for f in feats])
+        if diff_scale > 0:
+            sc[2] = diff_scale
+        assert np.allclose(rms.cpu().numpy(), sc, rtol=1e-12)
+        x_ref = np.concatenate([(f / s).reshape(nc, dpc).T for f, s in zip(feats, sc)], axis=0)
+        assert np.allclose(x.cpu().numpy(), x_ref, rtol=1e-6, atol=1e-6)
     base = rng.normal(0, 1, n)
-    for sign in (1.0, -1.0):
-        e = rng.normal(0, 1, n)
-        ae = sign * (0.5 * r + 0.1 * rng.normal(0, 1e-3, n))
+
+    def run(e, ae, f=None, af=None):
         out = torch.empty(n, dtype=torch.float64, device="cuda")
-        stats = torch.empty(4, dtype=torch.float64, device="cuda")
-        td = [torch.tensor(v, device="cuda") for v in (r, ae, e, base)]
-        E._check(E._lib.exg_dg_ls_step(*(E._ptr(v) for v in td), n, E._ptr(out), E._ptr(stats), E._stream()))
-        c = max(float(r @ ae) / float(ae @ ae), 0.0)
-        st = stats.cpu().numpy()
-        assert np.allclose(st[:3], [r @ ae, ae @ ae, r @ r], rtol=1e-12)
-        assert st[3] == pytest.approx(c, rel=1e-12, abs=0.0)
-        assert (c > 0) == (sign > 0)
-        assert np.allclose(out.cpu().numpy(), base + c * e, rtol=1e-14, atol=1e-14)
+        stats = torch.empty(6, dtype=torch.float64, device="cuda")
+        keep = [torch.tensor(v, device="cuda") if v is not None else None for v in (r, ae, e, af, f, base)]
+        ptrs = [None if v is None else E._ptr(v) for v in keep]
+        E._check(E._lib.exg_dg_ls_step(*ptrs, n, E._ptr(out), E._ptr(stats), E._stream()))
+        return out.cpu().numpy(), stats.cpu().numpy()
+
+    # one direction
+    e = rng.normal(0, 1, n)
+    ae = 0.5 * r + 1e-4 * rng.normal(0, 1, n)
+    out, st = run(e, ae)
+    c = float(r @ ae) / float(ae @ ae)
+    assert np.allclose(st[:3], [r @ ae, ae @ ae, r @ r], rtol=1e-12)
+    assert st[3] == pytest.approx(c, rel=1e-12) and st[4] == 0.0
+    assert np.allclose(out, base + c * e, rtol=1e-14, atol=1e-14)
+    # two directions: the normal equations
+    f = rng.normal(0, 1, n)
+    af = 0.3 * r + 2e-4 * rng.normal(0, 1, n)
+    out, st = run(e, ae, f, af)
+    M = np.array([[ae @ ae, ae @ af], [ae @ af, af @ af]])
+    ce, cf = np.linalg.solve(M, [r @ ae, r @ af])
+    assert st[3] == pytest.approx(ce, rel=1e-9) and st[4] == pytest.approx(cf, rel=1e-9)
+    res = r - ce * ae - cf * af
+    assert st[5] == pytest.approx(r @ r - res @ res, rel=1e-9)
+    assert np.allclose(out, base + ce * e + cf * f, rtol=1e-12, atol=1e-12)
+    # fallback: a correction orthogonal to the residual changes nothing
+    ao = rng.normal(0, 1, n)
+    ao -= (ao @ r) / (r @ r) * r
+    out, st = run(e, ao)
+    assert st[3] == 0.0 and st[4] == 0.0 and np.array_equal(out, base)

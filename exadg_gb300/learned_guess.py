@@ -22,6 +22,32 @@ import exadg_gb300 as E
 from exadg_gb300.cnn import CellPatchCNN
 
 
+def extrapolation_constants(order, time_steps=None, current_order=None):
+    """Weights beta_i of p_ext = sum_i beta_i p^{n-i} (ExtrapolationConstants,
+    time_integration/extrapolation_constants.cpp:55-150): Lagrange extrapolation through the last
+    `current_order` solutions to t_{n+1}, zero-padded to `order` entries (start-up with a lower
+    order).  time_steps[j] = t_{n+1-j} - t_{n-j} (time_steps[0] the step being taken); None means
+    constant steps.  With nodes tau_0 = 0, tau_i = -(dt_1 + ... + dt_i) relative to t_n and the
+    target dt_0: beta_i = prod_{j != i} (dt_0 - tau_j) / (tau_i - tau_j)."""
+    q = order if current_order is None else current_order
+    if not 1 <= q <= order <= 4:
+        raise ValueError("extrapolation order must be 1..4 and current order <= order")
+    dt = [1.0] * (q + 1) if time_steps is None else [float(v) for v in time_steps]
+    if len(dt) < q:
+        raise ValueError("need one time step per extrapolation node")
+    tau = [0.0]
+    for i in range(1, q):
+        tau.append(tau[-1] - dt[i])
+    beta = []
+    for i in range(q):
+        w = 1.0
+        for j in range(q):
+            if j != i:
+                w *= (dt[0] - tau[j]) / (tau[i] - tau[j])
+        beta.append(w)
+    return beta + [0.0] * (order - q)
+
+
 def _rms(t):
     import torch
 

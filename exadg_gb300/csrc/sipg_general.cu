@@ -341,6 +341,19 @@ __device__ __forceinline__ int fidx(int N, int d, int i, int p1, int p2) {
   return d == 0 ? i + N * (p1 + N * p2) : (d == 1 ? p1 + N * (i + N * p2) : p1 + N * (p2 + N * i));
 }
 
+// Per-cell strides of the shared arrays, padded so that the cell strides are congruent to the
+// N^2 threads of a cell modulo the 32 banks: consecutive threads of neighbouring cells in one warp
+// then address consecutive banks (no conflicts between the cells sharing a warp).
+template <int N, class C>
+__host__ __device__ constexpr int gen_pad(int len) {
+  constexpr int bank = 128 / (int)sizeof(C);
+  return len + (((N * N - len) % bank) + bank) % bank;
+}
+template <int N, class C>
+__host__ __device__ constexpr int gen_cell_stride() { return gen_pad<N, C>(N * N * N); }
+template <int N, class C>
+__host__ __device__ constexpr int gen_face_stride() { return gen_pad<N, C>(16 * N * N); }
+
 template <int N, int CPB, class T, class C>
 __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restrict__ src, T* __restrict__ dst,
                                                               const __grid_constant__ GenCoef<N, C> P,
@@ -350,13 +363,14 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
                                                               long long n_cells, long long n_dofs,
                                                               const PointEpilogue ep) {
   constexpr int N2 = N * N, N3 = N2 * N, NT = CPB * N2;
+  constexpr int SC = gen_cell_stride<N, C>(), SF = gen_face_stride<N, C>();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* su = reinterpret_cast<C*>(smem_raw);
-  C* so = su + CPB * N3;
-  C* t0 = so + CPB * N3;
-  C* t1 = t0 + CPB * N3;
-  C* t2 = t1 + CPB * N3;
-  C* fsh = t2 + CPB * N3;  // CPB * 16 * N2 face scratch
+  C* so = su + CPB * SC;
+  C* t0 = so + CPB * SC;
+  C* t1 = t0 + CPB * SC;
+  C* t2 = t1 + CPB * SC;
+  C* fsh = t2 + CPB * SC;  // CPB * SF face scratch
 
   // 1D matrices for the face stages, where the row index differs between the threads of a warp:
   // read from shared memory (a kernel-parameter read with a per-thread index is serialised)
@@ -374,14 +388,15 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
   const long long nch = min((long long)CPB, n_cells - c0);
   const int nd = (int)(nch * N3);
   for (int i = tid; i < CPB * N3; i += NT) {
-    su[i] = i < nd ? load_as<C>(s + base + i) : C(0);
-    so[i] = C(0);
+    const int lcc = i / N3, e = lcc * SC + i - lcc * N3;
+    su[e] = i < nd ? load_as<C>(s + base + i) : C(0);
+    so[e] = C(0);
   }
   __syncthreads();
   const int lc = tid / N2, l = tid - lc * N2, a = l % N, b = l / N;
   const bool active = lc < nch;
   const long long c = c0 + lc;
-  const int co = lc * N3;
+  const int co = lc * SC;
   C* U = su + co;
   C* A0 = t0 + co;
   C* A1 = t1 + co;
@@ -507,7 +522,7 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
   }
   __syncthreads();
   // ---- face terms
-  C* F = fsh + lc * 16 * N2;
+  C* F = fsh + lc * SF;
   C* fv = F;            // own trace value at face nodes
   C* fn = F + N2;       // own normal-direction derivative at face nodes
   C* gv = F + 2 * N2;   // neighbour trace value
@@ -652,7 +667,10 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
     }
     __syncthreads();
   }
-  for (int i = tid; i < nd; i += NT) epilogue_store<T>(ep, o, base + i, s, to_storage<T>(so[i]));
+  for (int i = tid; i < nd; i += NT) {
+    const int lcc = i / N3;
+    epilogue_store<T>(ep, o, base + i, s, to_storage<T>(so[lcc * SC + i - lcc * N3]));
+  }
 }
 
 template <int N, class C>
@@ -679,7 +697,7 @@ static void gen_apply_n(const GeneralGeom& g, const FE1D& fe, const void* src, v
                         const PointEpilogue& ep, long long cb, long long ce) {
   constexpr int CPB = gen_cpb<N>(), N3 = N * N * N, N2 = N * N;
   GenCoef<N, C> P = gen_coef<N, C>(fe);
-  size_t smem = (5 * (size_t)CPB * N3 + (size_t)CPB * 16 * N2) * sizeof(C);
+  size_t smem = (5 * (size_t)CPB * gen_cell_stride<N, C>() + (size_t)CPB * gen_face_stride<N, C>()) * sizeof(C);
   auto kern = gen_apply_kernel<N, CPB, T, C>;
   static bool attr_set = false;
   if (!attr_set) {

@@ -37,13 +37,6 @@ struct MapParams {
   int periodic[3];
 };
 
-__device__ void push_forward(const MapParams& P, const double X[3], double x[3]) {
-  double s = P.amp;
-  if (s != 0.0)
-    for (int e = 0; e < 3; ++e) s *= sin(P.freq * M_PI * (X[e] - P.left) / (P.right - P.left));
-  for (int e = 0; e < 3; ++e) x[e] = X[e] + s;
-}
-
 __device__ double lag(const double* z, int n, int i, double x) {
   double v = 1.0;
   for (int j = 0; j < n; ++j)
@@ -62,36 +55,36 @@ __device__ double lag_d(const double* z, int n, int i, double x) {
   return s;
 }
 
-// x(xi) and J(xi) of cell ci from the interpolated manifold
+// x(xi) and J(xi) of cell ci from the manifold interpolated at the (m+1)^3 mapping support points
+// (MappingQ of the deformed cube).  The deformation is separable, p_e(X) = X_e + amp prod_d S(X_d)
+// with S(t) = sin(freq pi (t - left) / (right - left)), so the interpolant factorises: with the 1D
+// Lagrange weights v_d(xi_d) of the support nodes, x_e = sum_a v_e,a X_e(a) + amp I_0 I_1 I_2 and
+// I_d = sum_a v_d,a S(X_d(a)) (the weights sum to one), and the Jacobian follows from the 1D
+// derivative weights.  3 (m+1) sines per point instead of 3 (m+1)^3.
 __device__ void map_eval(const MapParams& P, const int ci[3], const double xi[3], double x[3], double J[3][3]) {
-  double v[3][12], dv[3][12];
-  for (int e = 0; e < 3; ++e)
-    for (int a = 0; a < P.m1; ++a) {
-      v[e][a] = lag(P.nodes, P.m1, a, xi[e]);
-      dv[e][a] = lag_d(P.nodes, P.m1, a, xi[e]);
+  double I[3], dI[3], A[3], dA[3];
+  for (int d = 0; d < 3; ++d) {
+    double si = 0, dsi = 0, ai = 0, dai = 0;
+    for (int k = 0; k < P.m1; ++k) {
+      const double v = lag(P.nodes, P.m1, k, xi[d]), dv = lag_d(P.nodes, P.m1, k, xi[d]);
+      const double X = P.lo[d] + (ci[d] + P.nodes[k]) * P.h[d];
+      const double S = P.amp != 0.0 ? sin(P.freq * M_PI * (X - P.left) / (P.right - P.left)) : 0.0;
+      si += v * S;
+      dsi += dv * S;
+      ai += v * X;
+      dai += dv * X;
     }
-  for (int e = 0; e < 3; ++e) {
-    x[e] = 0;
-    J[e][0] = J[e][1] = J[e][2] = 0;
+    I[d] = si;
+    dI[d] = dsi;
+    A[d] = ai;
+    dA[d] = dai;
   }
-  for (int k = 0; k < P.m1; ++k)
-    for (int j = 0; j < P.m1; ++j)
-      for (int i = 0; i < P.m1; ++i) {
-        double X[3] = {P.lo[0] + (ci[0] + P.nodes[i]) * P.h[0], P.lo[1] + (ci[1] + P.nodes[j]) * P.h[1],
-                       P.lo[2] + (ci[2] + P.nodes[k]) * P.h[2]};
-        double p[3];
-        push_forward(P, X, p);
-        double w = v[0][i] * v[1][j] * v[2][k];
-        double w0 = dv[0][i] * v[1][j] * v[2][k];
-        double w1 = v[0][i] * dv[1][j] * v[2][k];
-        double w2 = v[0][i] * v[1][j] * dv[2][k];
-        for (int e = 0; e < 3; ++e) {
-          x[e] += w * p[e];
-          J[e][0] += w0 * p[e];
-          J[e][1] += w1 * p[e];
-          J[e][2] += w2 * p[e];
-        }
-      }
+  const double s = P.amp * I[0] * I[1] * I[2];
+  const double g[3] = {P.amp * dI[0] * I[1] * I[2], P.amp * I[0] * dI[1] * I[2], P.amp * I[0] * I[1] * dI[2]};
+  for (int e = 0; e < 3; ++e) {
+    x[e] = A[e] + s;
+    for (int d = 0; d < 3; ++d) J[e][d] = (e == d ? dA[d] : 0.0) + g[d];
+  }
 }
 
 __device__ double inv3(const double J[3][3], double Ji[3][3]) {

@@ -345,7 +345,7 @@ __host__ __device__ constexpr int gen_pad(int len) {
 template <int N, class C>
 __host__ __device__ constexpr int gen_cell_stride() { return gen_pad<N, C>(N * N * N); }
 template <int N, class C>
-__host__ __device__ constexpr int gen_face_stride() { return gen_pad<N, C>(16 * N * N); }
+__host__ __device__ constexpr int gen_face_stride() { return gen_pad<N, C>(28 * N * N); }
 
 template <int N, int CPB, class T, class C>
 __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restrict__ src, T* __restrict__ dst,
@@ -514,149 +514,263 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
     }
   }
   __syncthreads();
-  // ---- face terms
+  // ---- face terms, both faces of a direction per pass (independent work for the two faces in
+  // every stage, half the barriers).  Per face: traces (A), interpolation along t1 (1) and t2 plus
+  // the flux (2), transposed interpolation along t2 (E) and t1 with accumulation into the lines
+  // along d (F).  Each face has its own 14 N^2 scratch arrays.
   C* F = fsh + lc * SF;
-  C* fv = F;            // own trace value at face nodes
-  C* fn = F + N2;       // own normal-direction derivative at face nodes
-  C* gv = F + 2 * N2;   // neighbour trace value
-  C* gn = F + 3 * N2;   // neighbour normal derivative
-  C* r0 = F + 4 * N2;   // stage-1 buffers (q1, p2)
-  C* r1 = F + 5 * N2;
-  C* r2 = F + 6 * N2;
-  C* r3 = F + 7 * N2;
-  C* r4 = F + 8 * N2;
-  C* r5 = F + 9 * N2;
-  C* cv = F + 10 * N2;  // flux coefficients at face q
-  C* c0_ = F + 11 * N2;
-  C* c1_ = F + 12 * N2;
-  C* c2_ = F + 13 * N2;
   const int p1 = a, p2 = b;  // this thread's face point / node
 #pragma unroll 1
-  for (int f = 0; f < 6; ++f) {
-    const int d = f >> 1, side = f & 1;
+  for (int d = 0; d < 3; ++d) {
     int t1d, t2d;
     tang(d, t1d, t2d);
-    long long nb = active ? fnb[c * 6 + f] : -2;
-    const bool interior = nb >= 0;
-    const C* dside = side ? P.d1 : P.d0;
-    const C* dopp = side ? P.d0 : P.d1;
-    const int iend = side ? N - 1 : 0, iopp = side ? 0 : N - 1;
-    if (active) {
-      C nd = C(0);
-      for (int i = 0; i < N; ++i) nd = fmadd(dside[i], U[fidx(N, d, i, p1, p2)], nd);
-      fv[p2 * N + p1] = U[fidx(N, d, iend, p1, p2)];
-      fn[p2 * N + p1] = nd;
-      if (interior) {
-        const T* un = s + nb * N3;
-        C ndn = C(0);
-        for (int i = 0; i < N; ++i) ndn = fmadd(dopp[i], load_as<C>(un + fidx(N, d, i, p1, p2)), ndn);
-        gv[p2 * N + p1] = load_as<C>(un + fidx(N, d, iopp, p1, p2));
-        gn[p2 * N + p1] = ndn;
-      }
-    }
-    __syncthreads();
-    // stage 1 along t1: thread (q1 = p1, p2): contract over node index p1'
-    if (active && nb != -2) {
-      C sv = C(0), sdv = C(0), sn = 0, nv = C(0), ndv = 0, nn = C(0);
-      for (int k = 0; k < N; ++k) {
-        C Sq = sS[p1 * N + k], Dq = sD[p1 * N + k];
-        sv = fmadd(Sq, fv[p2 * N + k], sv);
-        sdv = fmadd(Dq, fv[p2 * N + k], sdv);
-        sn = fmadd(Sq, fn[p2 * N + k], sn);
+    const long long nbs[2] = {active ? fnb[c * 6 + 2 * d] : -2, active ? fnb[c * 6 + 2 * d + 1] : -2};
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      const int f = 2 * d + side;
+      const long long nb = nbs[side];
+      const bool interior = nb >= 0;
+      const C* dside = side ? P.d1 : P.d0;
+      const C* dopp = side ? P.d0 : P.d1;
+      const int iend = side ? N - 1 : 0, iopp = side ? 0 : N - 1;
+      C* Fs = F + side * 14 * N2;
+      C* fv = Fs;
+      C* fn = Fs + N2;
+      C* gv = Fs + 2 * N2;
+      C* gn = Fs + 3 * N2;
+      C* r0 = Fs + 4 * N2;
+      C* r1 = Fs + 5 * N2;
+      C* r2 = Fs + 6 * N2;
+      C* r3 = Fs + 7 * N2;
+      C* r4 = Fs + 8 * N2;
+      C* r5 = Fs + 9 * N2;
+      C* cv = Fs + 10 * N2;
+      C* c0_ = Fs + 11 * N2;
+      C* c1_ = Fs + 12 * N2;
+      C* c2_ = Fs + 13 * N2;
+      (void)f, (void)interior, (void)dside, (void)dopp, (void)iend, (void)iopp, (void)fv, (void)fn, (void)gv,
+          (void)gn, (void)r0, (void)r1, (void)r2, (void)r3, (void)r4, (void)r5, (void)cv, (void)c0_, (void)c1_,
+          (void)c2_;
+      if (active) {
+        C nd = C(0);
+        for (int i = 0; i < N; ++i) nd = fmadd(dside[i], U[fidx(N, d, i, p1, p2)], nd);
+        fv[p2 * N + p1] = U[fidx(N, d, iend, p1, p2)];
+        fn[p2 * N + p1] = nd;
         if (interior) {
-          nv = fmadd(Sq, gv[p2 * N + k], nv);
-          ndv = fmadd(Dq, gv[p2 * N + k], ndv);
-          nn = fmadd(Sq, gn[p2 * N + k], nn);
+          const T* un = s + nb * N3;
+          C ndn = C(0);
+          for (int i = 0; i < N; ++i) ndn = fmadd(dopp[i], load_as<C>(un + fidx(N, d, i, p1, p2)), ndn);
+          gv[p2 * N + p1] = load_as<C>(un + fidx(N, d, iopp, p1, p2));
+          gn[p2 * N + p1] = ndn;
         }
       }
-      r0[p2 * N + p1] = sv;
-      r1[p2 * N + p1] = sdv;
-      r2[p2 * N + p1] = sn;
-      r3[p2 * N + p1] = nv;
-      r4[p2 * N + p1] = ndv;
-      r5[p2 * N + p1] = nn;
     }
     __syncthreads();
-    // stage 2 along t2: thread (q1 = p1, q2 = p2): values / reference gradients at the face point,
-    // then the SIPG flux (laplace_operator.cpp:139-163 / 221-265)
-    if (active && nb != -2) {
-      C vo = C(0), go_t1 = C(0), go_t2 = 0, go_d = C(0), vn = 0, gn_t1 = C(0), gn_t2 = 0, gn_d = C(0);
-      for (int k = 0; k < N; ++k) {
-        C Sq = sS[p2 * N + k], Dq = sD[p2 * N + k];
-        vo = fmadd(Sq, r0[k * N + p1], vo);
-        go_t2 = fmadd(Dq, r0[k * N + p1], go_t2);
-        go_t1 = fmadd(Sq, r1[k * N + p1], go_t1);
-        go_d = fmadd(Sq, r2[k * N + p1], go_d);
-        if (interior) {
-          vn = fmadd(Sq, r3[k * N + p1], vn);
-          gn_t2 = fmadd(Dq, r3[k * N + p1], gn_t2);
-          gn_t1 = fmadd(Sq, r4[k * N + p1], gn_t1);
-          gn_d = fmadd(Sq, r5[k * N + p1], gn_d);
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      const int f = 2 * d + side;
+      const long long nb = nbs[side];
+      const bool interior = nb >= 0;
+      const C* dside = side ? P.d1 : P.d0;
+      const C* dopp = side ? P.d0 : P.d1;
+      const int iend = side ? N - 1 : 0, iopp = side ? 0 : N - 1;
+      C* Fs = F + side * 14 * N2;
+      C* fv = Fs;
+      C* fn = Fs + N2;
+      C* gv = Fs + 2 * N2;
+      C* gn = Fs + 3 * N2;
+      C* r0 = Fs + 4 * N2;
+      C* r1 = Fs + 5 * N2;
+      C* r2 = Fs + 6 * N2;
+      C* r3 = Fs + 7 * N2;
+      C* r4 = Fs + 8 * N2;
+      C* r5 = Fs + 9 * N2;
+      C* cv = Fs + 10 * N2;
+      C* c0_ = Fs + 11 * N2;
+      C* c1_ = Fs + 12 * N2;
+      C* c2_ = Fs + 13 * N2;
+      (void)f, (void)interior, (void)dside, (void)dopp, (void)iend, (void)iopp, (void)fv, (void)fn, (void)gv,
+          (void)gn, (void)r0, (void)r1, (void)r2, (void)r3, (void)r4, (void)r5, (void)cv, (void)c0_, (void)c1_,
+          (void)c2_;
+      if (active && nb != -2) {
+        C sv = C(0), sdv = C(0), sn = 0, nv = C(0), ndv = 0, nn = C(0);
+        for (int k = 0; k < N; ++k) {
+          C Sq = sS[p1 * N + k], Dq = sD[p1 * N + k];
+          sv = fmadd(Sq, fv[p2 * N + k], sv);
+          sdv = fmadd(Dq, fv[p2 * N + k], sdv);
+          sn = fmadd(Sq, fn[p2 * N + k], sn);
+          if (interior) {
+            nv = fmadd(Sq, gv[p2 * N + k], nv);
+            ndv = fmadd(Dq, gv[p2 * N + k], ndv);
+            nn = fmadd(Sq, gn[p2 * N + k], nn);
+          }
         }
+        r0[p2 * N + p1] = sv;
+        r1[p2 * N + p1] = sdv;
+        r2[p2 * N + p1] = sn;
+        r3[p2 * N + p1] = nv;
+        r4[p2 * N + p1] = ndv;
+        r5[p2 * N + p1] = nn;
       }
-      const C* fd = face + ((c * 6 + f) * N2 + p2 * N + p1) * 7;
-      C ao[3] = {fd[0], fd[1], fd[2]};
-      C JxW = fd[6];
-      C gref_o[3];
-      gref_o[d] = go_d;
-      gref_o[t1d] = go_t1;
-      gref_o[t2d] = go_t2;
-      C ndo = ao[0] * gref_o[0] + ao[1] * gref_o[1] + ao[2] * gref_o[2];
-      C tau = ftau[c * 6 + f];
-      C gflux, sv;
-      if (interior) {
-        C an[3] = {fd[3], fd[4], fd[5]};
-        C gref_n[3];
-        gref_n[d] = gn_d;
-        gref_n[t1d] = gn_t1;
-        gref_n[t2d] = gn_t2;
-        C ndn = an[0] * gref_n[0] + an[1] * gref_n[1] + an[2] * gref_n[2];
-        const bool own_minus = side == 1;
-        C um = own_minus ? vo : vn, up = own_minus ? vn : vo;
-        C nm = own_minus ? ndo : ndn, np = own_minus ? ndn : ndo;
-        gflux = cconst<C>(-0.5) * (um - up);
-        C vflux = cconst<C>(0.5) * (nm + np) - tau * (um - up);
-        sv = own_minus ? neg(vflux) : vflux;
-      } else {  // homogeneous Dirichlet: u+ = -u-, du+/dn = du-/dn
-        gflux = neg(vo);
-        sv = neg(ndo - cconst<C>(2.0) * tau * vo);
-      }
-      cv[p2 * N + p1] = JxW * sv;
-      C gj = JxW * gflux;
-      C cc[3] = {gj * ao[0], gj * ao[1], gj * ao[2]};
-      c0_[p2 * N + p1] = cc[d];
-      c1_[p2 * N + p1] = cc[t1d];
-      c2_[p2 * N + p1] = cc[t2d];
     }
     __syncthreads();
-    // integrate stage 1 along t2: thread (q1 = p1, node p2)
-    if (active && nb != -2) {
-      C s1 = C(0), s2 = C(0), s3 = 0, s4 = C(0);
-      for (int q = 0; q < N; ++q) {
-        C Sq = sS[q * N + p2], Dq = sD[q * N + p2];
-        s1 = fmadd(Sq, cv[q * N + p1], s1);
-        s2 = fmadd(Sq, c1_[q * N + p1], s2);
-        s3 = fmadd(Dq, c2_[q * N + p1], s3);
-        s4 = fmadd(Sq, c0_[q * N + p1], s4);
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      const int f = 2 * d + side;
+      const long long nb = nbs[side];
+      const bool interior = nb >= 0;
+      const C* dside = side ? P.d1 : P.d0;
+      const C* dopp = side ? P.d0 : P.d1;
+      const int iend = side ? N - 1 : 0, iopp = side ? 0 : N - 1;
+      C* Fs = F + side * 14 * N2;
+      C* fv = Fs;
+      C* fn = Fs + N2;
+      C* gv = Fs + 2 * N2;
+      C* gn = Fs + 3 * N2;
+      C* r0 = Fs + 4 * N2;
+      C* r1 = Fs + 5 * N2;
+      C* r2 = Fs + 6 * N2;
+      C* r3 = Fs + 7 * N2;
+      C* r4 = Fs + 8 * N2;
+      C* r5 = Fs + 9 * N2;
+      C* cv = Fs + 10 * N2;
+      C* c0_ = Fs + 11 * N2;
+      C* c1_ = Fs + 12 * N2;
+      C* c2_ = Fs + 13 * N2;
+      (void)f, (void)interior, (void)dside, (void)dopp, (void)iend, (void)iopp, (void)fv, (void)fn, (void)gv,
+          (void)gn, (void)r0, (void)r1, (void)r2, (void)r3, (void)r4, (void)r5, (void)cv, (void)c0_, (void)c1_,
+          (void)c2_;
+      if (active && nb != -2) {
+        C vo = C(0), go_t1 = C(0), go_t2 = 0, go_d = C(0), vn = 0, gn_t1 = C(0), gn_t2 = 0, gn_d = C(0);
+        for (int k = 0; k < N; ++k) {
+          C Sq = sS[p2 * N + k], Dq = sD[p2 * N + k];
+          vo = fmadd(Sq, r0[k * N + p1], vo);
+          go_t2 = fmadd(Dq, r0[k * N + p1], go_t2);
+          go_t1 = fmadd(Sq, r1[k * N + p1], go_t1);
+          go_d = fmadd(Sq, r2[k * N + p1], go_d);
+          if (interior) {
+            vn = fmadd(Sq, r3[k * N + p1], vn);
+            gn_t2 = fmadd(Dq, r3[k * N + p1], gn_t2);
+            gn_t1 = fmadd(Sq, r4[k * N + p1], gn_t1);
+            gn_d = fmadd(Sq, r5[k * N + p1], gn_d);
+          }
+        }
+        const C* fd = face + ((c * 6 + f) * N2 + p2 * N + p1) * 7;
+        C ao[3] = {fd[0], fd[1], fd[2]};
+        C JxW = fd[6];
+        C gref_o[3];
+        gref_o[d] = go_d;
+        gref_o[t1d] = go_t1;
+        gref_o[t2d] = go_t2;
+        C ndo = ao[0] * gref_o[0] + ao[1] * gref_o[1] + ao[2] * gref_o[2];
+        C tau = ftau[c * 6 + f];
+        C gflux, sv;
+        if (interior) {
+          C an[3] = {fd[3], fd[4], fd[5]};
+          C gref_n[3];
+          gref_n[d] = gn_d;
+          gref_n[t1d] = gn_t1;
+          gref_n[t2d] = gn_t2;
+          C ndn = an[0] * gref_n[0] + an[1] * gref_n[1] + an[2] * gref_n[2];
+          const bool own_minus = side == 1;
+          C um = own_minus ? vo : vn, up = own_minus ? vn : vo;
+          C nm = own_minus ? ndo : ndn, np = own_minus ? ndn : ndo;
+          gflux = cconst<C>(-0.5) * (um - up);
+          C vflux = cconst<C>(0.5) * (nm + np) - tau * (um - up);
+          sv = own_minus ? neg(vflux) : vflux;
+        } else {  // homogeneous Dirichlet: u+ = -u-, du+/dn = du-/dn
+          gflux = neg(vo);
+          sv = neg(ndo - cconst<C>(2.0) * tau * vo);
+        }
+        cv[p2 * N + p1] = JxW * sv;
+        C gj = JxW * gflux;
+        C cc[3] = {gj * ao[0], gj * ao[1], gj * ao[2]};
+        c0_[p2 * N + p1] = cc[d];
+        c1_[p2 * N + p1] = cc[t1d];
+        c2_[p2 * N + p1] = cc[t2d];
       }
-      r0[p2 * N + p1] = s1;
-      r1[p2 * N + p1] = s2;
-      r2[p2 * N + p1] = s3;
-      r3[p2 * N + p1] = s4;
     }
     __syncthreads();
-    // stage 2 along t1: thread (node p1, node p2) owns the line through it along d
-    if (active && nb != -2) {
-      C tv = C(0), tn = C(0);
-      for (int q = 0; q < N; ++q) {
-        C Sq = sS[q * N + p1], Dq = sD[q * N + p1];
-        tv = fmadd(Sq, r0[p2 * N + q], tv);
-        tv = fmadd(Dq, r1[p2 * N + q], tv);
-        tv = fmadd(Sq, r2[p2 * N + q], tv);
-        tn = fmadd(Sq, r3[p2 * N + q], tn);
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      const int f = 2 * d + side;
+      const long long nb = nbs[side];
+      const bool interior = nb >= 0;
+      const C* dside = side ? P.d1 : P.d0;
+      const C* dopp = side ? P.d0 : P.d1;
+      const int iend = side ? N - 1 : 0, iopp = side ? 0 : N - 1;
+      C* Fs = F + side * 14 * N2;
+      C* fv = Fs;
+      C* fn = Fs + N2;
+      C* gv = Fs + 2 * N2;
+      C* gn = Fs + 3 * N2;
+      C* r0 = Fs + 4 * N2;
+      C* r1 = Fs + 5 * N2;
+      C* r2 = Fs + 6 * N2;
+      C* r3 = Fs + 7 * N2;
+      C* r4 = Fs + 8 * N2;
+      C* r5 = Fs + 9 * N2;
+      C* cv = Fs + 10 * N2;
+      C* c0_ = Fs + 11 * N2;
+      C* c1_ = Fs + 12 * N2;
+      C* c2_ = Fs + 13 * N2;
+      (void)f, (void)interior, (void)dside, (void)dopp, (void)iend, (void)iopp, (void)fv, (void)fn, (void)gv,
+          (void)gn, (void)r0, (void)r1, (void)r2, (void)r3, (void)r4, (void)r5, (void)cv, (void)c0_, (void)c1_,
+          (void)c2_;
+      if (active && nb != -2) {
+        C s1 = C(0), s2 = C(0), s3 = 0, s4 = C(0);
+        for (int q = 0; q < N; ++q) {
+          C Sq = sS[q * N + p2], Dq = sD[q * N + p2];
+          s1 = fmadd(Sq, cv[q * N + p1], s1);
+          s2 = fmadd(Sq, c1_[q * N + p1], s2);
+          s3 = fmadd(Dq, c2_[q * N + p1], s3);
+          s4 = fmadd(Sq, c0_[q * N + p1], s4);
+        }
+        r0[p2 * N + p1] = s1;
+        r1[p2 * N + p1] = s2;
+        r2[p2 * N + p1] = s3;
+        r3[p2 * N + p1] = s4;
       }
-      so[co + fidx(N, d, iend, p1, p2)] = so[co + fidx(N, d, iend, p1, p2)] + tv;
-      for (int i = 0; i < N; ++i) so[co + fidx(N, d, i, p1, p2)] = fmadd(dside[i], tn, so[co + fidx(N, d, i, p1, p2)]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int side = 0; side < 2; ++side) {
+      const int f = 2 * d + side;
+      const long long nb = nbs[side];
+      const bool interior = nb >= 0;
+      const C* dside = side ? P.d1 : P.d0;
+      const C* dopp = side ? P.d0 : P.d1;
+      const int iend = side ? N - 1 : 0, iopp = side ? 0 : N - 1;
+      C* Fs = F + side * 14 * N2;
+      C* fv = Fs;
+      C* fn = Fs + N2;
+      C* gv = Fs + 2 * N2;
+      C* gn = Fs + 3 * N2;
+      C* r0 = Fs + 4 * N2;
+      C* r1 = Fs + 5 * N2;
+      C* r2 = Fs + 6 * N2;
+      C* r3 = Fs + 7 * N2;
+      C* r4 = Fs + 8 * N2;
+      C* r5 = Fs + 9 * N2;
+      C* cv = Fs + 10 * N2;
+      C* c0_ = Fs + 11 * N2;
+      C* c1_ = Fs + 12 * N2;
+      C* c2_ = Fs + 13 * N2;
+      (void)f, (void)interior, (void)dside, (void)dopp, (void)iend, (void)iopp, (void)fv, (void)fn, (void)gv,
+          (void)gn, (void)r0, (void)r1, (void)r2, (void)r3, (void)r4, (void)r5, (void)cv, (void)c0_, (void)c1_,
+          (void)c2_;
+      if (active && nb != -2) {
+        C tv = C(0), tn = C(0);
+        for (int q = 0; q < N; ++q) {
+          C Sq = sS[q * N + p1], Dq = sD[q * N + p1];
+          tv = fmadd(Sq, r0[p2 * N + q], tv);
+          tv = fmadd(Dq, r1[p2 * N + q], tv);
+          tv = fmadd(Sq, r2[p2 * N + q], tv);
+          tn = fmadd(Sq, r3[p2 * N + q], tn);
+        }
+        so[co + fidx(N, d, iend, p1, p2)] = so[co + fidx(N, d, iend, p1, p2)] + tv;
+        for (int i = 0; i < N; ++i) so[co + fidx(N, d, i, p1, p2)] = fmadd(dside[i], tn, so[co + fidx(N, d, i, p1, p2)]);
+      }
     }
     __syncthreads();
   }

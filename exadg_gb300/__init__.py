@@ -92,6 +92,7 @@ class CGDesc(ctypes.Structure):
         ("abs_tol", ctypes.c_double),
         ("rel_tol", ctypes.c_double),
         ("precond", ctypes.c_int),
+        ("device_loop", ctypes.c_int),
     ]
 
 
@@ -402,7 +403,8 @@ class KrylovSolver:
 
     NONE, JACOBI, MULTIGRID = 0, 1, 2
 
-    def __init__(self, operator, preconditioner=None, max_iter=10000, abs_tol=1e-20, rel_tol=1e-10, precond=None):
+    def __init__(self, operator, preconditioner=None, max_iter=10000, abs_tol=1e-20, rel_tol=1e-10, precond=None,
+                 device_loop=True):
         self.operator = operator
         self.preconditioner = preconditioner
         d = CGDesc()
@@ -413,6 +415,7 @@ class KrylovSolver:
         if precond is None:
             precond = self.MULTIGRID if preconditioner is not None else self.NONE
         d.precond = precond
+        d.device_loop = int(device_loop)
         self.desc = d
         self.result = None
 

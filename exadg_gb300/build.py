@@ -24,6 +24,7 @@ SOURCES = [
     "sipg_cartesian.cu",
     "sipg_general.cu",
     "solver_kernels.cu",
+    "cg_device.cu",
     "vec_ops.cu",
     "fe_tables.cpp",
     "host.cpp",

@@ -252,6 +252,7 @@ exg_status exg_cg_default_desc(exg_cg_desc* d) {
   d->abs_tol = 1e-20;
   d->rel_tol = 1e-10;
   d->precond = 2;
+  d->device_loop = 1;
   EXG_API_END
 }
 

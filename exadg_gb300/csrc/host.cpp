@@ -220,7 +220,12 @@ CGWorkspace& exg_op::workspace() {
 }
 
 CGWorkspace::~CGWorkspace() {
-  for (double* ptr : {r, z, p, v, dinv})
+  if (exec) cudaGraphExecDestroy(exec);
+  if (graph) cudaGraphDestroy(graph);
+  if (cap) cudaStreamDestroy(cap);
+  if (st_host) cudaFreeHost(st_host);
+  if (st) cudaFree(st);
+  for (double* ptr : {r, z, p, v, dinv, xw, bw})
     if (ptr) cudaFree(ptr);
   red.destroy();
 }
@@ -507,6 +512,12 @@ exg_mg::exg_mg(const exg_op& fine, const exg_mg_desc& d) : desc(d) {
       EXG_CUDA(cudaMemset(coarse_x, 0, L.n * cb));
       its_dev = (long long*)dalloc(sizeof(long long));
       EXG_CUDA(cudaMemset(its_dev, 0, sizeof(long long)));
+      if (prec == EXG_PREC_F32 && coarse_prec == EXG_PREC_F32)
+        coarse_cg_prepare<float, float>(n_coarse);
+      else if (prec == EXG_PREC_F32)
+        coarse_cg_prepare<float, double>(n_coarse);
+      else
+        coarse_cg_prepare<double, double>(n_coarse);
     }
   }
   EXG_CUDA(cudaDeviceSynchronize());
@@ -639,13 +650,22 @@ void exg_mg::vmult(const double* src, double* dst, cudaStream_t s) {
       EXG_CUDA(cudaStreamEndCapture(cap_stream, &graph));
       EXG_CUDA(cudaGraphInstantiate(&graph_exec, graph, 0));
       EXG_CUDA(cudaEventDestroy(ev));
+      graph_result = F.sol;  // every replay ends in the buffer the capture ended in
     }
     EXG_CUDA(cudaGraphLaunch(graph_exec, s));
+    vec_copy_convert(graph_result, prec, dst, EXG_PREC_F64, F.n, s);
   } else {
     run_vcycle(s);
+    vec_copy_convert(F.sol, prec, dst, EXG_PREC_F64, F.n, s);
   }
-  vec_copy_convert(F.sol, prec, dst, EXG_PREC_F64, F.n, s);
   ++vcycles;
+}
+
+void exg_mg::enqueue_vmult(const double* src, double* dst, cudaStream_t s) {
+  MGLevel& F = lv.back();
+  vec_copy_convert(src, EXG_PREC_F64, F.def, prec, F.n, s);
+  run_vcycle(s);
+  vec_copy_convert(F.sol, prec, dst, EXG_PREC_F64, F.n, s);
 }
 
 void exg_mg::info(exg_mg_info& out) const {
@@ -666,6 +686,108 @@ void exg_mg::info(exg_mg_info& out) const {
 // ============================================================================================
 // outer CG
 // ============================================================================================
+// Graph-driven PCG: x and b are copied into fixed work vectors, the initial residual is checked
+// on the host (as the host loop does), then one launch of a graph whose WHILE node repeats the
+// captured iteration until cg_check_kernel reports convergence, the iteration cap or a
+// non-finite residual.  The graph is captured on the first call with a given preconditioner.
+static exg_status cg_solve_device(exg_op& op, exg_mg* mg, const exg_cg_desc& d, const double* b, double* x,
+                                  exg_cg_result& res, cudaStream_t s) {
+  const long long n = op.n_dofs();
+  CGWorkspace& w = op.workspace();
+  Reduction& red = w.red;
+  if (!w.xw) {
+    w.xw = (double*)dalloc(n * 8);
+    w.bw = (double*)dalloc(n * 8);
+    w.st = (CGDevState*)dalloc(sizeof(CGDevState));
+    EXG_CUDA(cudaMallocHost(&w.st_host, sizeof(CGDevState)));
+    EXG_CUDA(cudaStreamCreateWithFlags(&w.cap, cudaStreamNonBlocking));
+  }
+  const void* want_mg = d.precond == 2 ? (const void*)mg : nullptr;
+  if (w.exec && (w.graph_mg != want_mg || w.graph_precond != d.precond)) {
+    cudaGraphExecDestroy(w.exec);
+    cudaGraphDestroy(w.graph);
+    w.exec = nullptr;
+    w.graph = nullptr;
+  }
+  const double* dinv = d.precond == 1 ? w.dinv : nullptr;
+  if (!w.exec) {
+    op.apply(w.r, w.v, 1, s);  // first launches (kernel attributes) happen outside the capture
+    EXG_CUDA(cudaStreamSynchronize(s));
+    EXG_CUDA(cudaGraphCreate(&w.graph, 0));
+    cudaGraphConditionalHandle h;
+    EXG_CUDA(cudaGraphConditionalHandleCreate(&h, w.graph, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams cp = {};
+    cp.type = cudaGraphNodeTypeConditional;
+    cp.conditional.handle = h;
+    cp.conditional.type = cudaGraphCondTypeWhile;
+    cp.conditional.size = 1;
+    cudaGraphNode_t node;
+    EXG_CUDA(cudaGraphAddNode(&node, w.graph, nullptr, nullptr, 0, &cp));
+    cudaGraph_t body = cp.conditional.phGraph_out[0];
+    EXG_CUDA(cudaStreamBeginCaptureToGraph(w.cap, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+    double *r = w.r, *z = w.z, *p = w.p, *v = w.v;
+    const double* out = red.out;
+    if (d.precond == 2) {
+      mg->enqueue_vmult(r, z, w.cap);
+      dot<double>(r, z, n, red, 4, w.cap);
+    } else {
+      precond_dot<double>(dinv, r, z, n, red, 4, w.cap);
+    }
+    cg_rho(w.st, out + 4, w.cap);
+    cg_p_update(z, p, w.st, n, w.cap);
+    op.apply(p, v, 1, w.cap);
+    dot<double>(p, v, n, red, 2, w.cap);
+    cg_alpha(w.st, out + 2, w.cap);
+    xr_update_dev(w.xw, r, p, v, &w.st->alpha, n, red, 3, w.cap);
+    cg_check(w.st, out + 3, h, w.cap);
+    cudaGraph_t captured;
+    EXG_CUDA(cudaStreamEndCapture(w.cap, &captured));
+    EXG_CUDA(cudaGraphInstantiate(&w.exec, w.graph, 0));
+    w.graph_mg = want_mg;
+    w.graph_precond = d.precond;
+  }
+  EXG_CUDA(cudaStreamSynchronize(s));
+  auto t0 = std::chrono::steady_clock::now();
+  EXG_CUDA(cudaMemcpyAsync(w.xw, x, n * 8, cudaMemcpyDeviceToDevice, s));
+  EXG_CUDA(cudaMemcpyAsync(w.bw, b, n * 8, cudaMemcpyDeviceToDevice, s));
+  // initial residual, as pcg_run
+  dot<double>(w.xw, w.xw, n, red, 0, s);
+  const bool xzero = read_slot(red, 0, s) == 0.0;
+  if (xzero) {
+    residual<double>(w.bw, nullptr, w.r, n, red, 1, s);
+  } else {
+    op.apply(w.xw, w.v, 1, s);
+    residual<double>(w.bw, w.v, w.r, n, red, 1, s);
+  }
+  const double r0 = std::sqrt(read_slot(red, 1, s));
+  const double tol = std::max(d.abs_tol, d.rel_tol * r0);
+  CGDevState& h = *w.st_host;
+  h = CGDevState{};
+  h.rn = r0;
+  h.tol = tol;
+  h.max_iter = d.max_iter;
+  h.status = !std::isfinite(r0) ? 2 : (r0 <= tol ? 0 : (d.max_iter <= 0 ? 1 : -1));
+  if (h.status < 0) {
+    EXG_CUDA(cudaMemcpyAsync(w.st, &h, sizeof(CGDevState), cudaMemcpyHostToDevice, s));
+    EXG_CUDA(cudaGraphLaunch(w.exec, s));
+    EXG_CUDA(cudaMemcpyAsync(&h, w.st, sizeof(CGDevState), cudaMemcpyDeviceToHost, s));
+  }
+  EXG_CUDA(cudaMemcpyAsync(x, w.xw, n * 8, cudaMemcpyDeviceToDevice, s));
+  EXG_CUDA(cudaStreamSynchronize(s));
+  auto t1 = std::chrono::steady_clock::now();
+  if (mg && d.precond == 2) mg->vcycles += h.it;
+  res.iterations = h.it;
+  res.converged = h.status == 0;
+  res.r0 = r0;
+  res.rn = h.rn;
+  res.rho = h.it > 0 && r0 > 0 ? std::pow(h.rn / r0, 1.0 / h.it) : 0.0;
+  res.n10 = (res.rho > 0 && res.rho < 1) ? -10.0 * std::log(10.0) / std::log(res.rho) : 0.0;
+  res.seconds = std::chrono::duration<double>(t1 - t0).count();
+  if (h.status == 2) return EXG_ERR_NONFINITE;
+  if (h.status == 1) return EXG_ERR_NOT_CONVERGED;
+  return EXG_OK;
+}
+
 exg_status exg::cg_solve(exg_op& op, exg_mg* mg, const exg_cg_desc& d, const double* b, double* x, exg_cg_result& res,
                          cudaStream_t s) {
   long long n = op.n_dofs();
@@ -681,6 +803,7 @@ exg_status exg::cg_solve(exg_op& op, exg_mg* mg, const exg_cg_desc& d, const dou
     }
     dinv = w.dinv;
   }
+  if (d.device_loop) return cg_solve_device(op, mg, d, b, x, res, s);
   EXG_CUDA(cudaStreamSynchronize(s));
   auto t0 = std::chrono::steady_clock::now();
   auto A = [&](const double* in, double* out) { op.apply(in, out, 1, s); };

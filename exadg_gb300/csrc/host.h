@@ -4,6 +4,7 @@
 #include <memory>
 #include <vector>
 
+#include "cg_device.h"
 #include "general.h"
 #include "internal.h"
 #include "solver_kernels.h"
@@ -23,6 +24,15 @@ struct CGWorkspace {
   double *r = nullptr, *z = nullptr, *p = nullptr, *v = nullptr, *dinv = nullptr;
   bool dinv_valid = false;
   Reduction red;
+  // graph-driven loop: the iteration body captured under a WHILE node on fixed vectors
+  double *xw = nullptr, *bw = nullptr;
+  CGDevState* st = nullptr;
+  CGDevState* st_host = nullptr;  // pinned
+  cudaStream_t cap = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  const void* graph_mg = nullptr;  // preconditioner the graph was captured with
+  int graph_precond = -1;
   ~CGWorkspace();
 };
 
@@ -101,11 +111,14 @@ struct exg_mg {
   cudaStream_t cap_stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t graph_exec = nullptr;
+  void* graph_result = nullptr;  // finest-level solution buffer the captured V-cycle ends in
   long long vcycles = 0;
 
   exg_mg(const exg_op& fine, const exg_mg_desc& d);
   ~exg_mg();
   void vmult(const double* src, double* dst, cudaStream_t s);
+  // dst = V-cycle(src) enqueued without a graph launch, for capture into a larger graph
+  void enqueue_vmult(const double* src, double* dst, cudaStream_t s);
   void info(exg_mg_info& out) const;
 
  private:

@@ -133,6 +133,29 @@ __global__ void xr_update_kernel(T* __restrict__ x, T* __restrict__ r, const T* 
   finish_reduction(s, red, slot);
 }
 
+// as xr_update_kernel with alpha read from device memory (graph-driven CG)
+__global__ void xr_update_dev_kernel(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
+                                     const double* __restrict__ v, const double* __restrict__ alpha_ptr, long long n,
+                                     Reduction red, int slot) {
+  __shared__ double sh[32];
+  const double alpha = *alpha_ptr;
+  double s = 0;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x) {
+    x[i] += alpha * p[i];
+    double ri = r[i] - alpha * v[i];
+    r[i] = ri;
+    s += ri * ri;
+  }
+  s = block_sum(s, sh);
+  finish_reduction(s, red, slot);
+}
+
+void xr_update_dev(double* x, double* r, const double* p, const double* v, const double* alpha, long long n,
+                   Reduction& red, int slot, cudaStream_t s) {
+  xr_update_dev_kernel<<<RED_BLOCKS, RED_THREADS, 0, s>>>(x, r, p, v, alpha, n, red, slot);
+  EXG_CUDA(cudaGetLastError());
+}
+
 template <class T>
 void dot(const T* x, const T* y, long long n, Reduction& red, int slot, cudaStream_t s) {
   dot_kernel<T><<<RED_BLOCKS, RED_THREADS, 0, s>>>(x, y, n, red, slot);
@@ -545,6 +568,18 @@ __global__ void __launch_bounds__(1024) coarse_cg_kernel(const CT* __restrict__ 
   if (tid == 0) its_counter[0] += it;
 }
 
+// raises the kernel's shared-memory limit for n unknowns (idempotent; call outside stream capture)
+template <class T, class CT>
+void coarse_cg_prepare(int n) {
+  size_t vec_bytes = 5 * (size_t)n * sizeof(CT), mat_bytes = (size_t)n * n * sizeof(CT);
+  size_t smem = vec_bytes + (vec_bytes + mat_bytes <= 200 * 1024 ? mat_bytes : 0);
+  static int attr_bytes = 0;
+  if ((int)smem > attr_bytes) {
+    EXG_CUDA(cudaFuncSetAttribute(coarse_cg_kernel<T, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    attr_bytes = (int)smem;
+  }
+}
+
 template <class T, class CT>
 void coarse_cg(const CT* A, const CT* invd, const T* rhs, T* x, CT* xstate, int n, double rel_tol, double abs_tol,
                int max_iter, int singular, long long* its, cudaStream_t s) {
@@ -552,11 +587,7 @@ void coarse_cg(const CT* A, const CT* invd, const T* rhs, T* x, CT* xstate, int 
   const int stage = vec_bytes + mat_bytes <= 200 * 1024 ? 1 : 0;
   size_t smem = vec_bytes + (stage ? mat_bytes : 0);
   auto k = coarse_cg_kernel<T, CT>;
-  static int attr_bytes = 0;
-  if ((int)smem > attr_bytes) {
-    EXG_CUDA(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_bytes = (int)smem;
-  }
+  coarse_cg_prepare<T, CT>(n);
   // one thread per unknown (whole warps, at most 1024): idle threads would only add FP64 work to
   // every block reduction
   const int threads = std::min(1024, std::max(32, (n + 31) / 32 * 32));
@@ -593,6 +624,9 @@ INST(float)
 INST(double)
 template void coarse_cg<float, float>(const float*, const float*, const float*, float*, float*, int, double, double,
                                       int, int, long long*, cudaStream_t);
+template void coarse_cg_prepare<float, float>(int);
+template void coarse_cg_prepare<float, double>(int);
+template void coarse_cg_prepare<double, double>(int);
 template void coarse_cg<float, double>(const double*, const double*, const float*, float*, double*, int, double,
                                        double, int, int, long long*, cudaStream_t);
 template void coarse_cg<double, double>(const double*, const double*, const double*, double*, double*, int, double,

@@ -159,6 +159,9 @@ typedef struct {
   double abs_tol;      /* 1e-20 */
   double rel_tol;      /* 1e-10 */
   int precond;         /* 0 none, 1 point Jacobi, 2 multigrid (mg handle) */
+  int device_loop;     /* 1: the iterations run as one CUDA-graph launch (a WHILE node over the
+                        * captured iteration, scalars and stopping test on the device); 0: host
+                        * loop reading the reductions each iteration.  Same arithmetic. */
 } exg_cg_desc;
 
 typedef struct {

@@ -120,3 +120,40 @@ def test_cg_reports_nonfinite_and_max_iter():
     s2 = E.KrylovSolver(op, None, precond=E.KrylovSolver.JACOBI)
     s2.solve(x, b, raise_on_failure=False)
     assert s2.result["status"] == E.EXG_ERR_NONFINITE
+
+
+@pytest.mark.parametrize("precond", [E.KrylovSolver.MULTIGRID, E.KrylovSolver.JACOBI, E.KrylovSolver.NONE])
+@pytest.mark.parametrize("warm", [False, True])
+def test_device_loop_matches_host_loop(precond, warm):
+    """The graph-driven CG (WHILE node, scalars on the device) takes the iterations of the host loop
+    and returns the same solution; repeated solves replay the captured graph, and a change of
+    preconditioner re-captures it."""
+    torch = require_gpu()
+    p, m = sine(3, False)
+    op = E.LaplaceOperator(m, 3)
+    mg = E.MultigridPreconditioner(op, mg_precision=E.PREC_F64) if precond == E.KrylovSolver.MULTIGRID else None
+    b = to_dev(torch, p.rhs(O.FN_SINE, np.pi))
+    for rep in range(2):
+        x0 = to_dev(torch, 0.1 * splitmix_uniform(p.n_dofs, 7 + rep)) if warm else op.initialize_dof_vector()
+        xs = []
+        its = []
+        for device_loop in (False, True):
+            x = x0.clone()
+            s = E.KrylovSolver(op, mg, precond=precond, device_loop=device_loop, max_iter=2000)
+            its.append(s.solve(x, b))
+            xs.append(x)
+        assert its[0] == its[1]
+        assert float(torch.linalg.norm(xs[0] - xs[1]) / torch.linalg.norm(xs[0])) <= 1e-13
+
+
+def test_device_loop_status_codes():
+    torch = require_gpu()
+    op = E.LaplaceOperator(E.Mesh(4), 2)
+    b = to_dev(torch, splitmix_uniform(op.n_dofs, 1))
+    x = op.initialize_dof_vector()
+    s = E.KrylovSolver(op, None, precond=E.KrylovSolver.JACOBI, max_iter=3, device_loop=True)
+    s.solve(x, b, raise_on_failure=False)
+    assert s.result["status"] == E.EXG_ERR_NOT_CONVERGED and s.result["iterations"] == 3
+    x.zero_()
+    s.solve(x, torch.zeros_like(b), raise_on_failure=False)  # converged at iteration 0
+    assert s.result["status"] == 0 and s.result["iterations"] == 0

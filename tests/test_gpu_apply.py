@@ -172,3 +172,40 @@ def test_apply_host_vectors(prec, kind, slabs):
     assert rel(yh.numpy(), p.apply(x)) <= 1e-12
     yd = op.vmult(op.initialize_dof_vector(), to_dev(torch, x))
     assert torch.equal(yd.cpu(), yh)
+
+
+TINY = [dict(n_cells=(1, 1, 1)), dict(n_cells=(1, 1, 1), periodic=(1, 1, 1)),
+        dict(n_cells=(1, 3, 2), periodic=(1, 0, 1), bc=(0, 0, 1, 0, 0, 0)), dict(n_cells=(5, 1, 1), periodic=(0, 1, 0)),
+        dict(n_cells=(2, 1, 3), bc=(1, 0, 0, 1, 0, 0)),
+        dict(n_cells=(1, 2, 1), deform_amp=0.1, deform_freq=1, mapping_degree=2)]
+
+
+@pytest.mark.parametrize("prec", [E.PREC_F64, E.PREC_F32, E.PREC_F64E])
+@pytest.mark.parametrize("mesh", range(len(TINY)))
+@pytest.mark.parametrize("k", [1, 3])
+def test_apply_tiny_and_ragged_meshes(prec, mesh, k):
+    """Single-cell and one-cell-thick meshes (a periodic direction of one cell is its own
+    neighbour), blocks larger than the mesh, every launch variant, the host-vector apply."""
+    torch = require_gpu()
+    kw = TINY[mesh]
+    p = O.Problem(O.mesh_desc(**kw), k)
+    op = E.LaplaceOperator(E.Mesh(**kw), k, 1.0, prec)
+    dt = torch.float32 if prec == E.PREC_F32 else torch.float64
+    x = splitmix_uniform(p.n_dofs, 5)
+    if prec == E.PREC_F32:
+        x = x.astype(np.float32).astype(np.float64)
+    ref = p.apply(x)
+    tol = 1e-5 if prec == E.PREC_F32 else 1e-12
+    xd = to_dev(torch, x, dt)
+    variants = [v for v, _ in op.tune()[1]] if op.cartesian else [0]
+    for v in variants:
+        if op.cartesian:
+            op.set_launch_config(v)
+        y = op.vmult(op.initialize_dof_vector(), xd)
+        assert rel(y.cpu().numpy(), ref) <= tol, v
+    if prec != E.PREC_F32:
+        xh = torch.tensor(x).pin_memory()
+        yh = torch.empty_like(xh).pin_memory()
+        op.vmult_host(yh, xh, n_slabs=4)
+        torch.cuda.synchronize()
+        assert rel(yh.numpy(), ref) <= tol

@@ -540,15 +540,20 @@ def run_learned(args):
     rhs, dt = LG.tgv_rhs_sequence(steps, n_cells=32, degree=2)
     gen_s = time.perf_counter() - t0
     res = {}
+    # plain_fp64: the reference's set-up on the GPU (FP64 operator, FP64 multigrid, BDF2 extrapolation)
+    runs = {"plain_fp64": ("extrapolation", E.PREC_F64, E.PREC_F64)}
     for mode in ("extrapolation", "extrapolation3", "untrained", "learned"):
-        seq = LG.PressureSequence(n_cells=32, degree=2, mode=mode, train_every=20, epochs=args.learned_epochs)
+        runs[mode] = (mode, E.PREC_F64E, E.PREC_F32)
+    for name, (mode, outer, mgp) in runs.items():
+        seq = LG.PressureSequence(n_cells=32, degree=2, mode=mode, train_every=20, epochs=args.learned_epochs,
+                                  outer_precision=outer, mg_precision=mgp)
         seq.diagnostics = args.learned_diagnostics
         for b in rhs:
             seq.step(b)
         log = seq.log
         tail = [r for r in log if r["step"] >= steps // 2]
         allw = [r for r in log if r["step"] >= 3]
-        res[mode] = {
+        res[name] = {
             "mean_iterations_after_step3": statistics.mean(r["iterations"] for r in allw),
             "mean_iterations_second_half": statistics.mean(r["iterations"] for r in tail),
             "mean_solve_s_second_half": statistics.mean(r["solve_s"] for r in tail),
@@ -563,14 +568,15 @@ def run_learned(args):
         }
         d3 = [r["r_ext3_rel"] for r in tail if "r_ext3_rel" in r]
         if d3:
-            res[mode]["mean_r_ext3_rel_second_half"] = statistics.mean(d3)
+            res[name]["mean_r_ext3_rel_second_half"] = statistics.mean(d3)
         last = [r for r in log if "loss_last" in r]
         if last:
-            res[mode]["loss_first_round"] = last[0]["loss_first"]
-            res[mode]["loss_last_round"] = last[-1]["loss_last"]
+            res[name]["loss_first_round"] = last[0]["loss_first"]
+            res[name]["loss_last_round"] = last[-1]["loss_last"]
         del seq
         torch.cuda.synchronize()
     e, l, u, e3 = res["extrapolation"], res["learned"], res["untrained"], res["extrapolation3"]
+    pf = res["plain_fp64"]
     line = {"metric": "PPE CG iterations per solve, learned guess vs BDF2 extrapolation (TGV 32^3, k_p=2)",
             "value": l["mean_iterations_second_half"], "unit": "iterations", "higher_is_better": False,
             "mode": "learned", "data": "synthetic: TGV Re=1600 pressure sources from a pseudo-spectral integrator",
@@ -578,6 +584,7 @@ def run_learned(args):
             "iteration_gain_second_half": e["mean_iterations_second_half"] - l["mean_iterations_second_half"],
             "iteration_gain_trained_vs_untrained": u["mean_iterations_second_half"] - l["mean_iterations_second_half"],
             "time_gain_second_half": e["mean_total_s_second_half"] / l["mean_total_s_second_half"],
+            "speedup_mixed_learned_vs_plain_fp64": pf["mean_total_s_second_half"] / l["mean_total_s_second_half"],
             "iteration_gain_vs_third_order_ls": e3["mean_iterations_second_half"] - l["mean_iterations_second_half"],
             "time_gain_vs_third_order_ls": e3["mean_total_s_second_half"] / l["mean_total_s_second_half"],
             "results": res}

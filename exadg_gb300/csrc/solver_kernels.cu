@@ -235,17 +235,25 @@ void rsub(const T* b, T* t, long long n, cudaStream_t s) {
 // multigrid's own number type.  A block handles G consecutive cells; for h-transfers the 1D matrix
 // of each direction is the one of the cell's child position in its parent.
 // ------------------------------------------------------------------------------------------------
-template <int NF>
+// cells per block.  Large levels: enough fine values per block (~4096) to amortise the three
+// barrier-separated sweeps, within 40 KB of static shared memory for the larger (restriction)
+// footprint.  Small levels (fewer than 8 blocks per SM at that size): ~512 fine values per block.
+template <int NF, int NC, class T>
 struct TransferShape {
-  static constexpr int G = 512 / (NF * NF * NF) < 1 ? 1 : 512 / (NF * NF * NF);  // cells per block
+  static constexpr int per_cell = NF * NF * NF + NF * NF * NC + NF * NC * NC + NC * NC * NC;
+  static constexpr int by_work = 4096 / (NF * NF * NF);
+  static constexpr int by_smem = (40 * 1024 / (int)sizeof(T) - 2 * NF * NC) / per_cell;
+  static constexpr int G0 = by_work < by_smem ? by_work : by_smem;
+  static constexpr int large = G0 < 1 ? 1 : G0;
+  static constexpr int small = 512 / (NF * NF * NF) < 1 ? 1 : 512 / (NF * NF * NF);
+  static bool use_large(long long cells) { return cells >= (long long)large * 152 * 8; }
 };
 
-template <int NF, int NC, class T>
+template <int NF, int NC, int G, class T>
 __global__ void __launch_bounds__(256) prolongate_kernel(const __grid_constant__ TransferParams P,
                                                          const T* __restrict__ coarse, T* __restrict__ fine,
                                                          long long n_cells) {
   constexpr int nf = NF, nc = NC, nf2 = nf * nf, nf3 = nf2 * nf, nc2 = nc * nc, nc3 = nc2 * nc;
-  constexpr int G = TransferShape<NF>::G;
   __shared__ T Ps[2 * nf * nc];  // [child][nf][nc]
   __shared__ T u[G * nc3];       // [G][nc3]
   __shared__ T t1[G * nc2 * nf];  // [G][c2][c1][i0]
@@ -307,12 +315,11 @@ __global__ void __launch_bounds__(256) prolongate_kernel(const __grid_constant__
   }
 }
 
-template <int NF, int NC, class T>
+template <int NF, int NC, int G, class T>
 __global__ void __launch_bounds__(256) restrict_kernel(const __grid_constant__ TransferParams P,
                                                        const T* __restrict__ fine, T* __restrict__ coarse,
                                                        long long n_cells) {
   constexpr int nf = NF, nc = NC, nf2 = nf * nf, nf3 = nf2 * nf, nc2 = nc * nc, nc3 = nc2 * nc;
-  constexpr int G = TransferShape<NF>::G;
   __shared__ T Ps[2 * nf * nc];    // [child][nf][nc]
   __shared__ T f[G * nf3];         // [G][nf3]
   __shared__ T t1[G * nf2 * nc];   // [G][i2][i1][j0]
@@ -379,8 +386,13 @@ void prolongate_add(const TransferParams& P, const T* coarse, T* fine, cudaStrea
   long long cells = (long long)P.Nf[0] * P.Nf[1] * P.Nf[2];
 #define EXG_PROLONG(NF, NC)                                                                        \
   if (P.nf == NF && P.nc == NC) {                                                                  \
-    constexpr int G = TransferShape<NF>::G;                                                        \
-    prolongate_kernel<NF, NC, T><<<(unsigned)((cells + G - 1) / G), 256, 0, s>>>(P, coarse, fine, cells); \
+    using S = TransferShape<NF, NC, T>;                                                            \
+    if (S::use_large(cells))                                                                       \
+      prolongate_kernel<NF, NC, S::large, T>                                                       \
+          <<<(unsigned)((cells + S::large - 1) / S::large), 256, 0, s>>>(P, coarse, fine, cells);  \
+    else                                                                                           \
+      prolongate_kernel<NF, NC, S::small, T>                                                       \
+          <<<(unsigned)((cells + S::small - 1) / S::small), 256, 0, s>>>(P, coarse, fine, cells);  \
     EXG_CUDA(cudaGetLastError());                                                                  \
     return;                                                                                        \
   }
@@ -393,8 +405,13 @@ void restrict_add(const TransferParams& P, const T* fine, T* coarse, cudaStream_
   long long cells = (long long)P.Nc[0] * P.Nc[1] * P.Nc[2];
 #define EXG_RESTRICT(NF, NC)                                                                       \
   if (P.nf == NF && P.nc == NC) {                                                                  \
-    constexpr int G = TransferShape<NF>::G;                                                        \
-    restrict_kernel<NF, NC, T><<<(unsigned)((cells + G - 1) / G), 256, 0, s>>>(P, fine, coarse, cells); \
+    using S = TransferShape<NF, NC, T>;                                                            \
+    if (S::use_large(cells))                                                                       \
+      restrict_kernel<NF, NC, S::large, T>                                                         \
+          <<<(unsigned)((cells + S::large - 1) / S::large), 256, 0, s>>>(P, fine, coarse, cells);  \
+    else                                                                                           \
+      restrict_kernel<NF, NC, S::small, T>                                                         \
+          <<<(unsigned)((cells + S::small - 1) / S::small), 256, 0, s>>>(P, fine, coarse, cells);  \
     EXG_CUDA(cudaGetLastError());                                                                  \
     return;                                                                                        \
   }

@@ -497,12 +497,8 @@ void exg_cnn::forward(const float* x, float* out, bool keep, cudaStream_t s) {
 void exg_cnn::wgrad(int K, const float* in, const float* g, int cin, int cout, float* gW, float* gb, cudaStream_t s) {
   int K3 = K * K * K;
   size_t smem = ((size_t)cout + K3) * (chunk + 1) * 4;
-  static int attr = 0;
-  if ((int)smem > attr) {
-    EXG_CUDA(cudaFuncSetAttribute(conv_wgrad_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
-    EXG_CUDA(cudaFuncSetAttribute(conv_wgrad_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, 64 * 1024));
-    attr = 64 * 1024;
-  }
+  ensure_smem_attr((const void*)conv_wgrad_kernel<3>, 64 * 1024);
+  ensure_smem_attr((const void*)conv_wgrad_kernel<1>, 64 * 1024);
   EXG_CHECK(smem <= 64 * 1024, EXG_ERR_UNSUPPORTED, "cnn: weight-gradient tile too large");
   dim3 grid(n_chunks, cin);
   if (K == 1)

@@ -119,5 +119,8 @@ std::vector<int> cart_cpb_options(int n, int precision);
 void vec_copy_convert(const void* src, int src_prec, void* dst, int dst_prec, long long n, cudaStream_t s);
 void vec_fill(void* x, int prec, double v, long long n, cudaStream_t s);
 void device_fma_peaks(double* f64_tflops, double* f32_tflops, cudaStream_t s);
+// raises a kernel's dynamic shared-memory limit to at least `bytes` on the current device (the
+// attribute is per device; thread-safe, a no-op once set)
+void ensure_smem_attr(const void* kernel, int bytes);
 
 }  // namespace exg

@@ -655,11 +655,7 @@ static void launch_apply(const CartHost& h, const void* src, void* dst, int n_rh
   CartCoef<N, C> P = make_coef<N, C>(h);
   size_t smem = smem_head_bytes<C>(CPB) + 4 * (size_t)CPB * N3 * sizeof(C);
   auto kern = cart_apply_kernel<N, CPB, T, C>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    EXG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = true;
-  }
+  ensure_smem_attr((const void*)kern, (int)smem);
   long long blocks = (h.mesh.cell_end - h.mesh.cell_begin + CPB - 1) / CPB;
   EXG_CHECK(blocks < (1LL << 31), EXG_ERR_INVALID, "mesh too large");
   EXG_CHECK(n_rhs >= 1 && n_rhs <= 65535, EXG_ERR_INVALID, "n_rhs out of range");
@@ -676,12 +672,8 @@ static void launch_brick(const CartHost& h, const void* src, void* dst, int n_rh
   CartCoef<N, C> P = make_coef<N, C>(h);
   size_t smem = brick_head_bytes<C>(Bk::NOWN, Bk::NSLOT) + ((size_t)Bk::NSLOT + 3 * Bk::NOWN) * N3 * sizeof(C);
   auto kern = cart_brick_kernel<N, BX, BY, BZ, T, C>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    EXG_CHECK(smem <= 227 * 1024, EXG_ERR_UNSUPPORTED, "brick too large for shared memory");
-    EXG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = true;
-  }
+  EXG_CHECK(smem <= 227 * 1024, EXG_ERR_UNSUPPORTED, "brick too large for shared memory");
+  ensure_smem_attr((const void*)kern, (int)smem);
   int nb[3] = {(h.mesh.N[0] + BX - 1) / BX, (h.mesh.N[1] + BY - 1) / BY, (h.mesh.N[2] + BZ - 1) / BZ};
   long long blocks = (long long)nb[0] * nb[1] * nb[2];
   EXG_CHECK(blocks < (1LL << 31), EXG_ERR_INVALID, "mesh too large");

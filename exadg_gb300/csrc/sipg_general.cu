@@ -806,11 +806,7 @@ static void gen_apply_n(const GeneralGeom& g, const FE1D& fe, const void* src, v
   GenCoef<N, C> P = gen_coef<N, C>(fe);
   size_t smem = (5 * (size_t)CPB * gen_cell_stride<N, C>() + (size_t)CPB * gen_face_stride<N, C>()) * sizeof(C);
   auto kern = gen_apply_kernel<N, CPB, T, C>;
-  static bool attr_set = false;
-  if (!attr_set) {
-    EXG_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_set = true;
-  }
+  ensure_smem_attr((const void*)kern, (int)smem);
   long long blocks = (ce - cb + CPB - 1) / CPB;
   dim3 grid((unsigned)blocks, (unsigned)n_rhs);
   kern<<<grid, CPB * N2, smem, s>>>((const T*)src, (T*)dst, P, (const C*)g.cellG, (const C*)g.face, (const C*)g.ftau,

@@ -590,11 +590,7 @@ template <class T, class CT>
 void coarse_cg_prepare(int n) {
   size_t vec_bytes = 5 * (size_t)n * sizeof(CT), mat_bytes = (size_t)n * n * sizeof(CT);
   size_t smem = vec_bytes + (vec_bytes + mat_bytes <= 200 * 1024 ? mat_bytes : 0);
-  static int attr_bytes = 0;
-  if ((int)smem > attr_bytes) {
-    EXG_CUDA(cudaFuncSetAttribute(coarse_cg_kernel<T, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    attr_bytes = (int)smem;
-  }
+  ensure_smem_attr((const void*)coarse_cg_kernel<T, CT>, (int)smem);
 }
 
 template <class T, class CT>

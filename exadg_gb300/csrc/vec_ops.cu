@@ -1,4 +1,8 @@
-// Streaming vector kernels: precision conversion and fills.
+// Streaming vector kernels: precision conversion and fills; per-device kernel attributes.
+#include <map>
+#include <mutex>
+#include <utility>
+
 #include "internal.h"
 
 namespace exg {
@@ -82,6 +86,19 @@ static double fma_rate(int sms, cudaStream_t s) {
   cudaEventDestroy(e1);
   cudaFree(out);
   return 2.0 * 8 * (double)iters * blocks * threads / (best * 1e-3) / 1e12;  // TFLOP/s, FMA = 2
+}
+
+void ensure_smem_attr(const void* kernel, int bytes) {
+  static std::mutex mu;
+  static std::map<std::pair<const void*, int>, int> done;  // (kernel, device) -> bytes set
+  int dev = 0;
+  EXG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  int& have = done[{kernel, dev}];
+  if (bytes > have) {
+    EXG_CUDA(cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes));
+    have = bytes;
+  }
 }
 
 void device_fma_peaks(double* f64_tflops, double* f32_tflops, cudaStream_t s) {

@@ -207,6 +207,20 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr())
 
 
+def _sized(t, n, dtype, what):
+    """Rejects tensors the kernels would over-run or misread (size, dtype): raw pointers cross the
+    C ABI, so the checks happen here."""
+    import torch
+
+    if not isinstance(t, torch.Tensor):
+        raise ExgError(EXG_ERR_INVALID, "%s: expected a torch tensor" % what)
+    if t.dtype != dtype:
+        raise ExgError(EXG_ERR_INVALID, "%s: dtype %s, expected %s" % (what, t.dtype, dtype))
+    if t.numel() < n:
+        raise ExgError(EXG_ERR_INVALID, "%s: %d entries, expected %d" % (what, t.numel(), n))
+    return t
+
+
 def _host_ptr(t, dtype_name="float64"):
     import torch
 
@@ -297,7 +311,9 @@ class LaplaceOperator:
     def vmult(self, dst, src, n_rhs=1, stream=None):
         """dst = A src (dst overwritten), operator_base.cpp:156-168."""
         f = _lib.exg_sipg_apply_f32 if self.precision == PREC_F32 else _lib.exg_sipg_apply_f64
-        _check(f(self.h, _ptr(src), _ptr(dst), n_rhs, _stream(stream)))
+        n = self.n_dofs * n_rhs
+        _check(f(self.h, _ptr(_sized(src, n, self.dtype, "src")), _ptr(_sized(dst, n, self.dtype, "dst")), n_rhs,
+                 _stream(stream)))
         return dst
 
     apply = vmult
@@ -305,18 +321,26 @@ class LaplaceOperator:
     def vmult_host(self, dst_host, src_host, n_slabs=8, stream=None):
         """dst_host = A src_host for FP64 host tensors (pinned for copy/compute overlap); queued on
         `stream`, complete when it synchronises."""
+        import torch
+
+        for t, what in ((src_host, "src"), (dst_host, "dst")):
+            _sized(t, self.n_dofs, torch.float64, what)
         _check(_lib.exg_sipg_apply_host_f64(self.h, _host_ptr(src_host), _host_ptr(dst_host), n_slabs,
                                             _stream(stream)))
         return dst_host
 
     def residual(self, r, b, x, stream=None):
         """r = b - A x in one kernel (FP64-storage operators)."""
+        import torch
+
+        for t, what in ((r, "r"), (b, "b"), (x, "x")):
+            _sized(t, self.n_dofs, torch.float64, what)
         _check(_lib.exg_sipg_residual_f64(self.h, _ptr(b), _ptr(x), _ptr(r), _stream(stream)))
         return r
 
     def calculate_inverse_diagonal(self, diag, stream=None):
         f = _lib.exg_sipg_inverse_diagonal_f32 if self.precision == PREC_F32 else _lib.exg_sipg_inverse_diagonal_f64
-        _check(f(self.h, _ptr(diag), _stream(stream)))
+        _check(f(self.h, _ptr(_sized(diag, self.n_dofs, self.dtype, "diag")), _stream(stream)))
         return diag
 
     def tune(self, n_rhs=1, stream=None):
@@ -346,6 +370,15 @@ class LaplaceOperator:
 
     def rhs(self, f_cell=None, g_face=None, h_face=None, stream=None):
         """b = (f, v) - inhomogeneous boundary part, from function values at the quadrature points."""
+        import torch
+
+        ncp = ctypes.c_longlong()
+        nfp = ctypes.c_longlong()
+        _check(_lib.exg_sipg_quadrature_points(self.h, None, None, ctypes.byref(ncp), ctypes.byref(nfp),
+                                               _stream(stream)))
+        for t, n, what in ((f_cell, ncp.value, "f_cell"), (g_face, nfp.value, "g_face"), (h_face, nfp.value, "h_face")):
+            if t is not None:
+                _sized(t, n, torch.float64, what)
         b = self.initialize_dof_vector()
         _check(_lib.exg_sipg_rhs(self.h, _ptr(f_cell), _ptr(g_face), _ptr(h_face), _ptr(b), _stream(stream)))
         return b
@@ -383,7 +416,11 @@ class MultigridPreconditioner:
             self.h = None
 
     def vmult(self, dst, src, stream=None):
-        _check(_lib.exg_mg_vmult(self.h, _ptr(src), _ptr(dst), _stream(stream)))
+        import torch
+
+        n = self.operator.n_dofs
+        _check(_lib.exg_mg_vmult(self.h, _ptr(_sized(src, n, torch.float64, "src")),
+                                 _ptr(_sized(dst, n, torch.float64, "dst")), _stream(stream)))
         return dst
 
     def info(self):
@@ -421,6 +458,11 @@ class KrylovSolver:
 
     def solve(self, dst, rhs, stream=None, raise_on_failure=True):
         """Solve A dst = rhs with dst as the initial guess; returns the iteration count."""
+        import torch
+
+        n = self.operator.n_dofs
+        _sized(rhs, n, torch.float64, "rhs")
+        _sized(dst, n, torch.float64, "dst")
         r = CGResult()
         mg = self.preconditioner.h if self.preconditioner is not None else None
         st = _lib.exg_cg_solve(self.operator.h, mg, ctypes.byref(self.desc), _ptr(rhs), _ptr(dst), ctypes.byref(r),

@@ -209,3 +209,35 @@ def test_apply_tiny_and_ragged_meshes(prec, mesh, k):
         op.vmult_host(yh, xh, n_slabs=4)
         torch.cuda.synchronize()
         assert rel(yh.numpy(), ref) <= tol
+
+
+@pytest.mark.parametrize("prec", [E.PREC_F64, E.PREC_F32, E.PREC_F64E])
+@pytest.mark.parametrize("kind", ["mixed", "periodic", "curved"])
+@pytest.mark.parametrize("k", [1, 4])
+def test_every_dof_written_once_and_deterministic(prec, kind, k):
+    """Element-centric kernels write each DoF from exactly one thread: a destination pre-filled
+    with NaN is fully overwritten by every launch variant (and by the host-vector slabs), and
+    repeated applies are bitwise identical (no write races, no atomics)."""
+    torch = require_gpu()
+    p, m, op = pair(kind, 5, k, prec)
+    dt = torch.float32 if prec == E.PREC_F32 else torch.float64
+    x = to_dev(torch, splitmix_uniform(p.n_dofs, 13), dt)
+    variants = [v for v, _ in op.tune()[1]] if op.cartesian else [0]
+    first = None
+    for v in variants:
+        if op.cartesian:
+            op.set_launch_config(v)
+        outs = []
+        for _ in range(2):
+            y = torch.full_like(x, float("nan"))
+            op.vmult(y, x)
+            assert not torch.isnan(y).any(), v
+            outs.append(y)
+        assert torch.equal(outs[0], outs[1]), v
+        first = outs[0] if first is None else first
+    if prec != E.PREC_F32:
+        xh = x.cpu().pin_memory()
+        yh = torch.full_like(xh, float("nan")).pin_memory()
+        op.vmult_host(yh, xh, n_slabs=3)
+        torch.cuda.synchronize()
+        assert not torch.isnan(yh).any()

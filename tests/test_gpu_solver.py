@@ -157,3 +157,40 @@ def test_device_loop_status_codes():
     x.zero_()
     s.solve(x, torch.zeros_like(b), raise_on_failure=False)  # converged at iteration 0
     assert s.result["status"] == 0 and s.result["iterations"] == 0
+
+
+def test_inconsistent_singular_problem_reports_failure():
+    """A periodic (singular) problem whose right-hand side has a mean, solved without mean
+    projection: no solution exists; the solver stops at its iteration cap with a status instead
+    of hanging or faulting, in both loop variants."""
+    torch = require_gpu()
+    m = E.Mesh(4, periodic=(1, 1, 1))
+    op = E.LaplaceOperator(m, 2)
+    mg = E.MultigridPreconditioner(op, mg_precision=E.PREC_F64, singular=False, coarse_max_iter=200)
+    b = to_dev(torch, splitmix_uniform(op.n_dofs, 3) + 1.0)
+    for device_loop in (True, False):
+        x = op.initialize_dof_vector()
+        s = E.KrylovSolver(op, mg, max_iter=50, device_loop=device_loop)
+        s.solve(x, b, raise_on_failure=False)
+        assert s.result["status"] in (E.EXG_ERR_NOT_CONVERGED, E.EXG_ERR_NONFINITE)
+        assert s.result["iterations"] <= 50
+
+
+def test_mismatched_vectors_are_rejected():
+    """Raw pointers cross the C ABI, so the Python layer rejects vectors of the wrong size or type
+    before any kernel could over-run them."""
+    torch = require_gpu()
+    op = E.LaplaceOperator(E.Mesh(3), 2)
+    n = op.n_dofs
+    good = op.initialize_dof_vector()
+    for bad in (torch.zeros(n - 1, dtype=torch.float64, device="cuda"), torch.zeros(n, dtype=torch.float32, device="cuda")):
+        with pytest.raises(E.ExgError):
+            op.vmult(good, bad)
+        with pytest.raises(E.ExgError):
+            op.vmult(bad, good)
+        with pytest.raises(E.ExgError):
+            E.KrylovSolver(op, None, precond=E.KrylovSolver.JACOBI).solve(bad, good)
+    with pytest.raises(E.ExgError):
+        op.vmult(good, good, n_rhs=2)
+    with pytest.raises(E.ExgError):
+        op.vmult_host(torch.zeros(n - 1, dtype=torch.float64), torch.zeros(n, dtype=torch.float64))

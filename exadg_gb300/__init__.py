@@ -117,7 +117,7 @@ EXPORTED_SYMBOLS = [
     "exg_mg_create", "exg_mg_destroy", "exg_mg_vmult", "exg_mg_info_get", "exg_cg_default_desc", "exg_cg_solve",
     "exg_cg_solve_noalloc", "exg_device_fma_peaks", "exg_status_string", "exg_last_error",
     "exg_cnn_create", "exg_cnn_destroy", "exg_cnn_n_params", "exg_cnn_params", "exg_cnn_forward",
-    "exg_cnn_backward", "exg_cnn_train_step", "exg_cnn_adam", "exg_dg_pack", "exg_dg_unpack_add", "exg_dg_pack_diff",
+    "exg_cnn_backward", "exg_cnn_train_step", "exg_cnn_adam", "exg_cnn_optimizer_state", "exg_dg_pack", "exg_dg_unpack_add", "exg_dg_pack_diff",
     "exg_dg_features", "exg_dg_ls_step",
 ]
 
@@ -171,6 +171,7 @@ def load_library(path=LIB_PATH):
         "exg_cnn_backward": [P, P, P, P],
         "exg_cnn_train_step": [P, P, P, ctypes.c_float, ctypes.POINTER(ctypes.c_float), P],
         "exg_cnn_adam": [P, ctypes.c_float, P],
+        "exg_cnn_optimizer_state": [P, PP, PP, ctypes.POINTER(ctypes.POINTER(LL))],
         "exg_dg_pack": [P, P, I, I, LL, P, P],
         "exg_dg_unpack_add": [P, P, D, I, LL, P, P],
         "exg_dg_pack_diff": [P, P, D, I, LL, P, P],

@@ -51,6 +51,25 @@ class CellPatchCNN:
     def grads(self):
         return self._views()[1]
 
+    def optimizer_state(self):
+        """(first moments, second moments) as device views, and the Adam step count."""
+        import torch
+
+        m = ctypes.c_void_p()
+        v = ctypes.c_void_p()
+        st = ctypes.POINTER(ctypes.c_longlong)()
+        E._check(E._lib.exg_cnn_optimizer_state(self.h, ctypes.byref(m), ctypes.byref(v), ctypes.byref(st)))
+        return (torch.as_tensor(_CudaArray(m.value, self.n_params), device="cuda"),
+                torch.as_tensor(_CudaArray(v.value, self.n_params), device="cuda"), st)
+
+    @property
+    def adam_step(self):
+        return self.optimizer_state()[2][0]
+
+    @adam_step.setter
+    def adam_step(self, value):
+        self.optimizer_state()[2][0] = int(value)
+
     def layer_shapes(self):
         ci, ch, co = self.c_in, self.c_hidden, self.c_out
         return [("W1", (ch, ci)), ("b1", (ch,)), ("W2", (ch, ch, 27)), ("b2", (ch,)), ("W3", (co, ch, 27)),

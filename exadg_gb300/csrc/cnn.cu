@@ -633,6 +633,15 @@ exg_status exg_cnn_train_step(exg_cnn* cnn, const float* x, const float* target,
   CNN_END
 }
 
+exg_status exg_cnn_optimizer_state(exg_cnn* cnn, float** m, float** v, long long** step) {
+  CNN_BEGIN
+  EXG_CHECK(cnn && m && v && step, EXG_ERR_INVALID, "null argument");
+  *m = cnn->m;
+  *v = cnn->v;
+  *step = &cnn->step;
+  CNN_END
+}
+
 exg_status exg_cnn_adam(exg_cnn* cnn, float lr, void* stream) {
   CNN_BEGIN
   EXG_CHECK(cnn, EXG_ERR_INVALID, "null argument");

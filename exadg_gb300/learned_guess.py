@@ -97,6 +97,7 @@ class PressureSequence:
         self.delta_scale = None
         self.x = torch.empty((4 * self.dpc, self.nc), dtype=torch.float32, device="cuda")
         self.log = []
+        self.steps_done = 0
         n = self.op.n_dofs
         self.tmp = torch.empty(n, dtype=torch.float64, device="cuda")
         self.zero = torch.zeros(n, dtype=torch.float64, device="cuda")
@@ -252,7 +253,7 @@ class PressureSequence:
         torch.cuda.synchronize()
         t2 = time.perf_counter()
         info = self._resolve(info)
-        rec = dict(step=len(self.log), iterations=its, solve_s=t2 - t1, guess_s=t1 - t0, source=info["source"],
+        rec = dict(step=self.steps_done, iterations=its, solve_s=t2 - t1, guess_s=t1 - t0, source=info["source"],
                    r0_rel=solver.result["r0"] / bn)
         if "r_ext" in info:
             rec["r_ext_rel"] = info["r_ext"] / bn
@@ -265,7 +266,7 @@ class PressureSequence:
         self.hist.append(x)
         if len(self.hist) > 3:
             self.hist.pop(0)
-        if self.mode == "learned" and len(self.samples) > 0 and (len(self.log) + 1) % self.train_every == 0:
+        if self.mode == "learned" and len(self.samples) > 0 and (self.steps_done + 1) % self.train_every == 0:
             torch.cuda.synchronize()
             t3 = time.perf_counter()
             losses = self._train()
@@ -274,7 +275,78 @@ class PressureSequence:
             rec["loss_first"] = losses[0]
             rec["loss_last"] = losses[-1]
         self.log.append(rec)
+        self.steps_done += 1
         return x, rec
+
+    # ------------------------------------------------------------------------------------------
+    # checkpoint / restart (the state a time loop needs to continue: pressure history, network
+    # weights, Adam state, training buffer and scales), as one little-endian file with a header
+    _MAGIC = b"EXGPSEQ1"
+    _HEADER = "<8sqqqqqqqdq"  # magic, n_dofs, dofs/cell, cells, n_params, n_hist, n_samples, steps,
+    #                          delta_scale (NaN: none), flags (bit 0: trained)
+
+    def save(self, path):
+        import struct
+
+        import numpy as np
+
+        torch = self.torch
+        torch.cuda.synchronize()
+        n_params = self.cnn.n_params if self.cnn is not None else 0
+        ds = float("nan") if self.delta_scale is None else float(self.delta_scale)
+        with open(path, "wb") as f:
+            f.write(struct.pack(self._HEADER, self._MAGIC, self.op.n_dofs, self.dpc, self.nc, n_params,
+                                len(self.hist), len(self.samples), self.steps_done, ds, int(self.trained)))
+            for h in self.hist:
+                f.write(h.cpu().numpy().astype("<f8").tobytes())
+            if self.cnn is not None:
+                m, v, st = self.cnn.optimizer_state()
+                for t in (self.cnn.params, m, v):
+                    f.write(t.cpu().numpy().astype("<f4").tobytes())
+                f.write(np.array([st[0]], dtype="<i8").tobytes())
+            for x, r, d in self.samples:
+                f.write(x.cpu().numpy().astype("<f4").tobytes())
+                f.write(r.cpu().numpy().astype("<f8").tobytes())
+                f.write(d.cpu().numpy().astype("<f8").tobytes())
+
+    def load(self, path):
+        """Restores a state written by save() into a sequence built with the same mesh, degree
+        and mode."""
+        import struct
+
+        import numpy as np
+
+        torch = self.torch
+        with open(path, "rb") as f:
+            head = f.read(struct.calcsize(self._HEADER))
+            magic, n, dpc, nc, n_params, n_hist, n_samples, steps, ds, flags = struct.unpack(self._HEADER, head)
+            if magic != self._MAGIC:
+                raise ValueError("not a pressure-sequence checkpoint")
+            own_params = self.cnn.n_params if self.cnn is not None else 0
+            if (n, dpc, nc, n_params) != (self.op.n_dofs, self.dpc, self.nc, own_params):
+                raise ValueError("checkpoint was written for another mesh, degree or network")
+
+            def read(count, dtype):
+                a = np.frombuffer(f.read(count * np.dtype(dtype).itemsize), dtype=dtype)
+                if a.size != count:
+                    raise ValueError("truncated checkpoint")
+                return torch.from_numpy(a.astype(dtype[1:] if dtype[0] == "<" else dtype)).cuda()
+
+            self.hist = [read(n, "<f8") for _ in range(n_hist)]
+            if self.cnn is not None:
+                m, v, st = self.cnn.optimizer_state()
+                self.cnn.params.copy_(read(n_params, "<f4"))
+                m.copy_(read(n_params, "<f4"))
+                v.copy_(read(n_params, "<f4"))
+                st[0] = int(np.frombuffer(f.read(8), dtype="<i8")[0])
+            self.samples = []
+            for _ in range(n_samples):
+                self.samples.append((read(4 * dpc * nc, "<f4").view(4 * dpc, nc), read(n, "<f8"), read(n, "<f8")))
+        self.steps_done = steps
+        self.delta_scale = None if ds != ds else ds
+        self.trained = bool(flags & 1)
+        torch.cuda.synchronize()
+
 
 
 def tgv_rhs_sequence(n_steps, n_cells=32, degree=2, dt=None, modes=64, device="cuda"):

@@ -204,6 +204,9 @@ exg_status exg_cnn_train_step(exg_cnn* cnn, const float* x, const float* target,
                               void* stream);
 /* one Adam step with the gradient currently held by the network (from exg_cnn_backward) */
 exg_status exg_cnn_adam(exg_cnn* cnn, float lr, void* stream);
+/* the Adam state for checkpoints: device pointers to the first and second moments (n_params
+ * floats each) and a host pointer to the step counter (read / write) */
+exg_status exg_cnn_optimizer_state(exg_cnn* cnn, float** m, float** v, long long** step);
 /* x[j*dpc + i][c] = vecs[j][c*dpc + i] * inv_scales[j] (vecs, inv_scales: device arrays) */
 exg_status exg_dg_pack(const double* const* vecs, const double* inv_scales, int n_vec, int dofs_per_cell,
                        long long n_cells, float* x, void* stream);

@@ -128,3 +128,31 @@ def test_features_and_ls_step_on_device():
     ao -= (ao @ r) / (r @ r) * r
     out, st = run(e, ao)
     assert st[3] == 0.0 and st[4] == 0.0 and np.array_equal(out, base)
+
+
+def test_pressure_sequence_checkpoint_restart(tmp_path):
+    """Save after 20 steps, continue; a fresh sequence loaded from the file continues the same way
+    (history, weights, Adam moments and step, training buffer restored; the multigrid's coarse
+    warm start is not part of the state, so solutions agree to the solver tolerance)."""
+    torch = require_gpu()
+    from exadg_gb300 import learned_guess as LG
+
+    rhs, _ = LG.tgv_rhs_sequence(30, n_cells=8, degree=2, modes=32)
+    kw = dict(n_cells=8, degree=2, mode="learned", train_every=10, epochs=10)
+    a = LG.PressureSequence(**kw)
+    for b in rhs[:20]:
+        a.step(b)
+    path = str(tmp_path / "seq.bin")
+    a.save(path)
+    n_samples, trained = len(a.samples), a.trained
+    ref = [a.step(b) for b in rhs[20:]]
+    c = LG.PressureSequence(**kw)
+    c.load(path)
+    assert c.steps_done == 20 and c.trained == trained and len(c.samples) == n_samples
+    out = [c.step(b) for b in rhs[20:]]
+    for (xa, ra), (xc, rc) in zip(ref, out):
+        assert abs(ra["iterations"] - rc["iterations"]) <= 1
+        assert float(torch.linalg.norm(xa - xc)) <= 1e-7 * float(torch.linalg.norm(xa))
+    wrong = LG.PressureSequence(n_cells=6, degree=2, mode="learned")
+    with pytest.raises(ValueError):
+        wrong.load(path)

@@ -502,7 +502,11 @@ def run_component(args):
         z = torch.empty_like(r)
         run = lambda: mg.vmult(z, r)
         info = mg.info()
-        what = {"levels": [(l["n_cells"][0], l["degree"]) for l in info["levels"]], "mg_precision": "f32"}
+        for _ in range(2):
+            mg.level_timings(r)
+        level_ms = mg.level_timings(r)  # eager V-cycle with events per level (outside the timed region)
+        what = {"levels": [(l["n_cells"][0], l["degree"]) for l in info["levels"]], "mg_precision": "f32",
+                "eager_level_ms": level_ms}
     for _ in range(max(args.warmup, 3)):
         run()
     torch.cuda.synchronize()

@@ -114,7 +114,7 @@ EXPORTED_SYMBOLS = [
     "exg_sipg_info", "exg_sipg_tune", "exg_sipg_set_launch_config", "exg_sipg_apply_f64", "exg_sipg_apply_f32",
     "exg_sipg_residual_f64", "exg_sipg_apply_host_f64", "exg_sipg_inverse_diagonal_f64",
     "exg_sipg_inverse_diagonal_f32", "exg_sipg_quadrature_points", "exg_sipg_rhs", "exg_mg_default_desc",
-    "exg_mg_create", "exg_mg_destroy", "exg_mg_vmult", "exg_mg_info_get", "exg_cg_default_desc", "exg_cg_solve",
+    "exg_mg_create", "exg_mg_destroy", "exg_mg_vmult", "exg_mg_info_get", "exg_mg_level_timings", "exg_cg_default_desc", "exg_cg_solve",
     "exg_cg_solve_noalloc", "exg_device_fma_peaks", "exg_status_string", "exg_last_error",
     "exg_cnn_create", "exg_cnn_destroy", "exg_cnn_n_params", "exg_cnn_params", "exg_cnn_forward",
     "exg_cnn_backward", "exg_cnn_train_step", "exg_cnn_adam", "exg_cnn_optimizer_state", "exg_dg_pack", "exg_dg_unpack_add", "exg_dg_pack_diff",
@@ -159,6 +159,7 @@ def load_library(path=LIB_PATH):
         "exg_mg_destroy": [P],
         "exg_mg_vmult": [P, P, P, P],
         "exg_mg_info_get": [P, ctypes.POINTER(MGInfo)],
+        "exg_mg_level_timings": [P, P, P, ctypes.POINTER(ctypes.c_float), I, ctypes.POINTER(I), P],
         "exg_cg_default_desc": [ctypes.POINTER(CGDesc)],
         "exg_cg_solve": [P, P, ctypes.POINTER(CGDesc), P, P, ctypes.POINTER(CGResult), P],
         "exg_cg_solve_noalloc": [P, ctypes.POINTER(CGDesc), P, P, ctypes.POINTER(CGResult), P],
@@ -423,6 +424,18 @@ class MultigridPreconditioner:
         _check(_lib.exg_mg_vmult(self.h, _ptr(_sized(src, n, torch.float64, "src")),
                                  _ptr(_sized(dst, n, torch.float64, "dst")), _stream(stream)))
         return dst
+
+    def level_timings(self, src, dst=None, stream=None):
+        """ms per level (coarse first) of one eagerly run V-cycle on src."""
+        import torch
+
+        n = self.operator.n_dofs
+        _sized(src, n, torch.float64, "src")
+        dst = torch.empty_like(src) if dst is None else _sized(dst, n, torch.float64, "dst")
+        buf = (ctypes.c_float * 32)()
+        nl = ctypes.c_int()
+        _check(_lib.exg_mg_level_timings(self.h, _ptr(src), _ptr(dst), buf, 32, ctypes.byref(nl), _stream(stream)))
+        return [float(buf[i]) for i in range(nl.value)]
 
     def info(self):
         i = MGInfo()

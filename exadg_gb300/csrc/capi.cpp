@@ -238,6 +238,17 @@ exg_status exg_mg_vmult(exg_mg* mg, const double* src, double* dst, void* stream
   EXG_API_END
 }
 
+exg_status exg_mg_level_timings(exg_mg* mg, const double* src, double* dst, float* ms, int capacity,
+                                int* n_levels, void* stream) {
+  EXG_API_BEGIN
+  EXG_CHECK(mg && src && dst && n_levels, EXG_ERR_INVALID, "null argument");
+  std::vector<float> t;
+  mg->timed_vmult(src, dst, t, (cudaStream_t)stream);
+  *n_levels = (int)t.size();
+  for (int l = 0; l < (int)t.size() && l < capacity && ms; ++l) ms[l] = t[l];
+  EXG_API_END
+}
+
 exg_status exg_mg_info_get(const exg_mg* mg, exg_mg_info* info) {
   EXG_API_BEGIN
   EXG_CHECK(mg && info, EXG_ERR_INVALID, "null argument");

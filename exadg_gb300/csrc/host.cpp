@@ -587,6 +587,10 @@ void exg_mg::smooth(int l, bool zero_start, cudaStream_t s) {
 
 void exg_mg::v_cycle(int l, cudaStream_t s) {
   MGLevel& L = lv[l];
+  auto mark = [&](int k) {
+    if (tev) EXG_CUDA(cudaEventRecord((*tev)[4 * l + k], s));
+  };
+  mark(0);
   if (l == 0) {
     if (prec == EXG_PREC_F32 && coarse_prec == EXG_PREC_F32)
       coarse_cg<float, float>((const float*)coarseA, (const float*)coarse_invd, (const float*)L.def, (float*)L.sol,
@@ -600,6 +604,7 @@ void exg_mg::v_cycle(int l, cudaStream_t s) {
       coarse_cg<double, double>((const double*)coarseA, (const double*)coarse_invd, (const double*)L.def,
                                 (double*)L.sol, (double*)coarse_x, n_coarse, desc.coarse_rel_tol,
                                 desc.coarse_abs_tol, desc.coarse_max_iter, desc.singular, its_dev, s);
+    mark(1);
     return;
   }
   MGLevel& C = lv[l - 1];
@@ -621,12 +626,15 @@ void exg_mg::v_cycle(int l, cudaStream_t s) {
     restrict_add<float>(L.tr, (const float*)L.t, (float*)C.def, s);
   else
     restrict_add<double>(L.tr, (const double*)L.t, (double*)C.def, s);
+  mark(1);
   v_cycle(l - 1, s);
+  mark(2);
   if (prec == EXG_PREC_F32)
     prolongate_add<float>(L.tr, (const float*)C.sol, (float*)L.sol, s);
   else
     prolongate_add<double>(L.tr, (const double*)C.sol, (double*)L.sol, s);
   smooth(l, false, s);
+  mark(3);
 }
 
 void exg_mg::run_vcycle(cudaStream_t s) {
@@ -666,6 +674,34 @@ void exg_mg::enqueue_vmult(const double* src, double* dst, cudaStream_t s) {
   vec_copy_convert(src, EXG_PREC_F64, F.def, prec, F.n, s);
   run_vcycle(s);
   vec_copy_convert(F.sol, prec, dst, EXG_PREC_F64, F.n, s);
+}
+
+void exg_mg::timed_vmult(const double* src, double* dst, std::vector<float>& ms, cudaStream_t s) {
+  const int nl = (int)lv.size();
+  std::vector<cudaEvent_t> ev(4 * nl);
+  for (auto& e : ev) EXG_CUDA(cudaEventCreate(&e));
+  MGLevel& F = lv.back();
+  vec_copy_convert(src, EXG_PREC_F64, F.def, prec, F.n, s);
+  tev = &ev;
+  try {
+    run_vcycle(s);
+  } catch (...) {
+    tev = nullptr;
+    for (auto& e : ev) cudaEventDestroy(e);
+    throw;
+  }
+  tev = nullptr;
+  vec_copy_convert(F.sol, prec, dst, EXG_PREC_F64, F.n, s);
+  EXG_CUDA(cudaStreamSynchronize(s));
+  ms.assign(nl, 0.0f);
+  for (int l = 0; l < nl; ++l) {
+    float a = 0, b = 0;
+    EXG_CUDA(cudaEventElapsedTime(&a, ev[4 * l], ev[4 * l + 1]));
+    if (l > 0) EXG_CUDA(cudaEventElapsedTime(&b, ev[4 * l + 2], ev[4 * l + 3]));
+    ms[l] = a + b;
+  }
+  for (auto& e : ev) cudaEventDestroy(e);
+  ++vcycles;
 }
 
 void exg_mg::info(exg_mg_info& out) const {

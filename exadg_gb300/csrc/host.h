@@ -119,10 +119,14 @@ struct exg_mg {
   void vmult(const double* src, double* dst, cudaStream_t s);
   // dst = V-cycle(src) enqueued without a graph launch, for capture into a larger graph
   void enqueue_vmult(const double* src, double* dst, cudaStream_t s);
+  // one eager V-cycle with CUDA events around every level's work (smoothing, residual and
+  // transfers on the way down and up; the coarse solve); ms[l] for l = 0 (coarse) .. n_levels-1
+  void timed_vmult(const double* src, double* dst, std::vector<float>& ms, cudaStream_t s);
   void info(exg_mg_info& out) const;
 
  private:
   void v_cycle(int l, cudaStream_t s);
+  std::vector<cudaEvent_t>* tev = nullptr;  // 4 events per level while timed_vmult runs
   void smooth(int l, bool zero_start, cudaStream_t s);
   void run_vcycle(cudaStream_t s);
 };

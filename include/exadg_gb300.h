@@ -153,6 +153,13 @@ exg_status exg_mg_create(const exg_op* fine, const exg_mg_desc* desc, exg_mg** m
 exg_status exg_mg_destroy(exg_mg* mg);
 exg_status exg_mg_vmult(exg_mg* mg, const double* src, double* dst, void* stream);
 exg_status exg_mg_info_get(const exg_mg* mg, exg_mg_info* info);
+/* One V-cycle dst = M src run eagerly with CUDA events around each level's work (smoothing,
+ * residual and transfers on the way down and up; level 0 = the coarse solve); ms[l] receives the
+ * time of level l, coarse first, for up to `capacity` levels; *n_levels the number of levels.
+ * Synchronises `stream`.  The per-level timer of the reference's V-cycle
+ * (multigrid/multigrid_algorithm.h:41, 176-237, behind ENABLE_TIMING). */
+exg_status exg_mg_level_timings(exg_mg* mg, const double* src, double* dst, float* ms, int capacity,
+                                int* n_levels, void* stream);
 
 typedef struct {
   int max_iter;        /* 10000 */

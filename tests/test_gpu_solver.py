@@ -194,3 +194,21 @@ def test_mismatched_vectors_are_rejected():
         op.vmult(good, good, n_rhs=2)
     with pytest.raises(E.ExgError):
         op.vmult_host(torch.zeros(n - 1, dtype=torch.float64), torch.zeros(n, dtype=torch.float64))
+
+
+def test_level_timings_match_vcycle():
+    """The event-timed eager V-cycle gives the graph V-cycle's result and one positive time per
+    level."""
+    torch = require_gpu()
+    p, m = sine(3, False)
+    op = E.LaplaceOperator(m, 3)
+    mg = E.MultigridPreconditioner(op, mg_precision=E.PREC_F64)
+    r = to_dev(torch, splitmix_uniform(p.n_dofs, 4))
+    ms = mg.level_timings(r)
+    assert len(ms) == mg.info()["n_levels"] and all(t > 0 for t in ms)
+    mg2 = E.MultigridPreconditioner(op, mg_precision=E.PREC_F64)
+    a = mg2.vmult(op.initialize_dof_vector(), r)
+    mg3 = E.MultigridPreconditioner(op, mg_precision=E.PREC_F64)
+    b = torch.empty_like(r)
+    mg3.level_timings(r, b)
+    assert float(torch.linalg.norm(a - b) / torch.linalg.norm(a)) <= 1e-13

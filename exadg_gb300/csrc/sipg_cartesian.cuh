@@ -163,28 +163,33 @@ __device__ __forceinline__ void face_info(const CartMesh& m, const CartCoef<N, C
   int ci[3];
   cell_coords(m, c, ci);
   const int d = f >> 1, side = f & 1;
+  // direction-d quantities through selects: runtime indices into small arrays would live in
+  // local memory
   const int stride = d == 0 ? 1 : (d == 1 ? m.N[0] : m.N[0] * m.N[1]);
-  const int cd = ci[d];
+  const int cd = d == 0 ? ci[0] : (d == 1 ? ci[1] : ci[2]);
+  const int Nd = d == 0 ? m.N[0] : (d == 1 ? m.N[1] : m.N[2]);
+  const int per = d == 0 ? m.periodic[0] : (d == 1 ? m.periodic[1] : m.periodic[2]);
   const C tc = P.tauA[d][cell_class(m, ci)];
   nb = -1;
-  int cn[3] = {ci[0], ci[1], ci[2]};
+  int cdn = cd;
   if (side == 1) {
-    if (cd + 1 < m.N[d]) {
+    if (cd + 1 < Nd) {
       nb = c + stride;
-      cn[d] = cd + 1;
-    } else if (m.periodic[d]) {
-      nb = c - (m.N[d] - 1) * stride;
-      cn[d] = 0;
+      cdn = cd + 1;
+    } else if (per) {
+      nb = c - (Nd - 1) * stride;
+      cdn = 0;
     }
   } else {
     if (cd > 0) {
       nb = c - stride;
-      cn[d] = cd - 1;
-    } else if (m.periodic[d]) {
-      nb = c + (m.N[d] - 1) * stride;
-      cn[d] = m.N[d] - 1;
+      cdn = cd - 1;
+    } else if (per) {
+      nb = c + (Nd - 1) * stride;
+      cdn = Nd - 1;
     }
   }
+  const int cn[3] = {d == 0 ? cdn : ci[0], d == 1 ? cdn : ci[1], d == 2 ? cdn : ci[2]};
   if (nb >= 0) {
     kind = 0;
     atau = cmax(tc, P.tauA[d][cell_class(m, cn)]);
@@ -277,7 +282,7 @@ __device__ __forceinline__ void mass_line(C* __restrict__ x, int a, int b, const
 template <int N, int CPB, class T, class C>
 __global__ void __launch_bounds__(CPB* N* N) cart_apply_kernel(const T* __restrict__ src, T* __restrict__ dst,
                                                                const __grid_constant__ CartCoef<N, C> P,
-                                                               const CartMesh m, const PointEpilogue ep) {
+                                                               const __grid_constant__ CartMesh m, const PointEpilogue ep) {
   constexpr int N2 = N * N, N3 = N2 * N, NT = CPB * N2;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   C* stau = reinterpret_cast<C*>(smem_raw);             // CPB*6
@@ -436,7 +441,7 @@ __host__ __device__ constexpr size_t brick_head_bytes(int nown, int nslot) {
 template <int N, int BX, int BY, int BZ, class T, class C>
 __global__ void __launch_bounds__(BX* BY* BZ* N* N)
     cart_brick_kernel(const T* __restrict__ src, T* __restrict__ dst, const __grid_constant__ CartCoef<N, C> P,
-                      const CartMesh m, int nbx, int nby, const PointEpilogue ep) {
+                      const __grid_constant__ CartMesh m, int nbx, int nby, const PointEpilogue ep) {
   using B = Brick<BX, BY, BZ>;
   constexpr int N2 = N * N, N3 = N2 * N, NT = B::NOWN * N2;
   static_assert(NT >= 32, "brick needs at least one full warp");
@@ -597,7 +602,8 @@ __global__ void __launch_bounds__(BX* BY* BZ* N* N)
 // diagonal: sum_d diag(A_d L_d^self)[i_d] * M[i_e][i_e] * M[i_f][i_f]
 // (MatrixFreeTools::compute_diagonal via operator_base.cpp:618-646; inversion per invert_diagonal.h)
 template <int N, class T, class C>
-__global__ void cart_diag_kernel(T* __restrict__ diag, const __grid_constant__ CartCoef<N, C> P, const CartMesh m,
+__global__ void cart_diag_kernel(T* __restrict__ diag, const __grid_constant__ CartCoef<N, C> P,
+                                 const __grid_constant__ CartMesh m,
                                  bool invert) {
   constexpr int N3 = N * N * N;
   long long g = (long long)blockIdx.x * blockDim.x + threadIdx.x;

@@ -658,20 +658,20 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
         const C* fd = face + ((c * 6 + f) * N2 + p2 * N + p1) * 7;
         C ao[3] = {fd[0], fd[1], fd[2]};
         C JxW = fd[6];
-        C gref_o[3];
-        gref_o[d] = go_d;
-        gref_o[t1d] = go_t1;
-        gref_o[t2d] = go_t2;
-        C ndo = ao[0] * gref_o[0] + ao[1] * gref_o[1] + ao[2] * gref_o[2];
+        // reference gradient components by direction, through selects (a runtime index into a small
+        // array would put it in local memory)
+        const C go0 = d == 0 ? go_d : (t1d == 0 ? go_t1 : go_t2);
+        const C go1 = d == 1 ? go_d : (t1d == 1 ? go_t1 : go_t2);
+        const C go2 = d == 2 ? go_d : (t1d == 2 ? go_t1 : go_t2);
+        C ndo = ao[0] * go0 + ao[1] * go1 + ao[2] * go2;
         C tau = ftau[c * 6 + f];
         C gflux, sv;
         if (interior) {
           C an[3] = {fd[3], fd[4], fd[5]};
-          C gref_n[3];
-          gref_n[d] = gn_d;
-          gref_n[t1d] = gn_t1;
-          gref_n[t2d] = gn_t2;
-          C ndn = an[0] * gref_n[0] + an[1] * gref_n[1] + an[2] * gref_n[2];
+          const C gn0 = d == 0 ? gn_d : (t1d == 0 ? gn_t1 : gn_t2);
+          const C gn1 = d == 1 ? gn_d : (t1d == 1 ? gn_t1 : gn_t2);
+          const C gn2 = d == 2 ? gn_d : (t1d == 2 ? gn_t1 : gn_t2);
+          C ndn = an[0] * gn0 + an[1] * gn1 + an[2] * gn2;
           const bool own_minus = side == 1;
           C um = own_minus ? vo : vn, up = own_minus ? vn : vo;
           C nm = own_minus ? ndo : ndn, np = own_minus ? ndn : ndo;
@@ -684,10 +684,12 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
         }
         cv[p2 * N + p1] = JxW * sv;
         C gj = JxW * gflux;
-        C cc[3] = {gj * ao[0], gj * ao[1], gj * ao[2]};
-        c0_[p2 * N + p1] = cc[d];
-        c1_[p2 * N + p1] = cc[t1d];
-        c2_[p2 * N + p1] = cc[t2d];
+        const C a_d = d == 0 ? ao[0] : (d == 1 ? ao[1] : ao[2]);
+        const C a_t1 = t1d == 0 ? ao[0] : (t1d == 1 ? ao[1] : ao[2]);
+        const C a_t2 = t2d == 0 ? ao[0] : (t2d == 1 ? ao[1] : ao[2]);
+        c0_[p2 * N + p1] = gj * a_d;
+        c1_[p2 * N + p1] = gj * a_t1;
+        c2_[p2 * N + p1] = gj * a_t2;
       }
     }
     __syncthreads();

@@ -55,6 +55,7 @@ class SolverDesc(ctypes.Structure):
         ("coarse_double", ctypes.c_int),
         ("min_coarse_cells", ctypes.c_int),
         ("singular", ctypes.c_int),
+        ("mg_type", ctypes.c_int),
     ]
 
 
@@ -127,6 +128,20 @@ def lib():
         L.orc_transfer.argtypes = [ctypes.c_int, ctypes.c_int, I, I, ctypes.c_int, D, D]
         L.orc_fe1d.argtypes = [ctypes.c_int, D, D, D]
         L.orc_tridiag_eigs.argtypes = [ctypes.c_int, D, D, D]
+        L.orc_cg_create.restype = P
+        L.orc_cg_create.argtypes = [ctypes.POINTER(MeshDesc), ctypes.c_int, ctypes.c_int]
+        L.orc_cg_destroy.argtypes = [P]
+        L.orc_cg_n_dofs.restype = ctypes.c_long
+        L.orc_cg_n_dofs.argtypes = [P]
+        L.orc_cg_apply_f64.argtypes = [P, D, D]
+        L.orc_cg_apply_f32.argtypes = [P, F, F]
+        L.orc_cg_diagonal_f64.argtypes = [P, D]
+        L.orc_cg_constrained.argtypes = [P, ctypes.POINTER(ctypes.c_ubyte)]
+        L.orc_cg_dg_map.argtypes = [P, ctypes.POINTER(ctypes.c_long)]
+        L.orc_lattice_transfer.argtypes = [ctypes.POINTER(MeshDesc), I, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                           ctypes.c_int, ctypes.c_int, D, D]
+        L.orc_mg_level_dg.restype = ctypes.c_int
+        L.orc_mg_level_dg.argtypes = [P, ctypes.c_int]
         _lib = L
     return _lib
 
@@ -278,7 +293,8 @@ class Multigrid:
             lam = ctypes.c_double()
             its = ctypes.c_int()
             lib().orc_mg_level(self.h, l, N, ctypes.byref(deg), ctypes.byref(lam), ctypes.byref(its))
-            out.append(dict(n_cells=tuple(N), degree=deg.value, lambda_max=lam.value, eig_iters=its.value))
+            out.append(dict(n_cells=tuple(N), degree=deg.value, lambda_max=lam.value, eig_iters=its.value,
+                            dg=bool(lib().orc_mg_level_dg(self.h, l))))
         return out
 
     def coarse_iterations(self):
@@ -303,6 +319,68 @@ def transfer(kc, kf, n_coarse, n_fine, src, restrict=False):
     else:
         out = np.zeros(int(np.prod(n_fine)) * (kf + 1) ** 3)
     lib().orc_transfer(kc, kf, Nc, Nf, 1 if restrict else 0, _dp(src), _dp(out))
+    return out
+
+
+class ContinuousProblem:
+    """Continuous Q_k Laplace operator on the node lattice of a Cartesian mesh (cphMG levels)."""
+
+    def __init__(self, mesh, degree, singular=False):
+        self.mesh = mesh
+        self.degree = degree
+        self.h = lib().orc_cg_create(ctypes.byref(mesh), degree, int(singular))
+        self.n_dofs = lib().orc_cg_n_dofs(self.h)
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_cg_destroy(self.h)
+            self.h = None
+
+    def apply(self, src):
+        src = np.ascontiguousarray(src, dtype=np.float64)
+        dst = np.empty_like(src)
+        lib().orc_cg_apply_f64(self.h, _dp(src), _dp(dst))
+        return dst
+
+    def apply_f32(self, src):
+        src = np.ascontiguousarray(src, dtype=np.float32)
+        dst = np.empty_like(src)
+        lib().orc_cg_apply_f32(self.h, _fp(src), _fp(dst))
+        return dst
+
+    def diagonal(self):
+        out = np.empty(self.n_dofs)
+        lib().orc_cg_diagonal_f64(self.h, _dp(out))
+        return out
+
+    def constrained(self):
+        out = np.empty(self.n_dofs, dtype=np.uint8)
+        lib().orc_cg_constrained(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)))
+        return out.astype(bool)
+
+    def dg_map(self):
+        """lattice node of every DG DoF of the same mesh and degree"""
+        n = int(np.prod(list(self.mesh.n_cells))) * (self.degree + 1) ** 3
+        out = np.empty(n, dtype=np.int64)
+        lib().orc_cg_dg_map(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_long)))
+        return out
+
+
+def lattice_transfer(mesh, n_coarse, kc, kf, fine_dg, src, restrict=False, singular=False):
+    """Transfer between a continuous level (n_coarse cells, degree kc) and the level of ``mesh``
+    (degree kf; discontinuous when fine_dg): prolongate_and_add / restrict_and_add into zeros."""
+    Nc = (ctypes.c_int * 3)(*n_coarse)
+    mc = mesh_desc(tuple(n_coarse), lo=tuple(mesh.lo), hi=tuple(mesh.hi), periodic=tuple(mesh.periodic),
+                   bc=tuple(mesh.bc))
+    coarse_n = ContinuousProblem(mc, kc, singular).n_dofs
+    if fine_dg:
+        fine_n = int(np.prod(list(mesh.n_cells))) * (kf + 1) ** 3
+    else:
+        fine_n = ContinuousProblem(mesh, kf, singular).n_dofs
+    src = np.ascontiguousarray(src, dtype=np.float64)
+    out = np.zeros(coarse_n if restrict else fine_n)
+    lib().orc_lattice_transfer(ctypes.byref(mesh), Nc, kc, kf, int(fine_dg), int(singular), int(restrict),
+                               _dp(src), _dp(out))
     return out
 
 

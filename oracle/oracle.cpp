@@ -170,6 +170,7 @@ typedef struct {
   int coarse_double;     // 1: coarse CG in double even when the V-cycle is float
   int min_coarse_cells;  // stop h-coarsening at this many cells per direction (2)
   int singular;          // subtract mean in the coarse solve (pure Neumann / periodic)
+  int mg_type;           // 0: phMG (DG on every level), 1: cphMG (continuous levels below the finest)
 } orc_solver_desc;
 
 typedef struct {
@@ -453,8 +454,18 @@ enum OpType { HOMOGENEOUS = 0, INHOMOGENEOUS = 1, FULL = 2 };
 // cell / face / boundary loops; each cell integrates only its own test functions, which is the
 // reference's cell-based face-loop variant).
 // -------------------------------------------------------------------------------------------
+// what the multigrid levels need from an operator: the discontinuous SIPG operator (Laplace)
+// and the continuous one (ContinuousLaplace, cphMG levels) both provide it
 template <class Number>
-struct Laplace {
+struct LevelOp {
+  virtual ~LevelOp() {}
+  virtual long n_dofs() const = 0;
+  virtual void apply(const Number* src, Number* dst) const = 0;
+  virtual void diagonal(Number* diag) const = 0;
+};
+
+template <class Number>
+struct Laplace : LevelOp<Number> {
   std::shared_ptr<Geometry> geo;
   int k, n, nq;
   double ip;
@@ -463,7 +474,7 @@ struct Laplace {
   std::vector<Number> tau_cell;     // per cell penalty (surface / volume)
   Number tau_factor;                // (k+1)^2 * IP_factor
   long n_cells() const { return geo->mesh.n_cells(); }
-  long n_dofs() const { return n_cells() * n * n * n; }
+  long n_dofs() const override { return n_cells() * n * n * n; }
 
   void init(std::shared_ptr<Geometry> g, int degree, double ip_factor) {
     geo = g;
@@ -729,7 +740,7 @@ struct Laplace {
   }
 
   // OperatorBase::apply (zero_dst = true), operator_base.cpp:264-310
-  void apply(const Number* src, Number* dst) const {
+  void apply(const Number* src, Number* dst) const override {
     long nc = n_cells(), n3 = (long)n * n * n;
 #pragma omp parallel
     {
@@ -775,7 +786,7 @@ struct Laplace {
   }
 
   // diagonal by sum factorisation (cell + own-side face terms), MatrixFreeTools::compute_diagonal
-  void diagonal(Number* diag) const {
+  void diagonal(Number* diag) const override {
     const Mesh& m = geo->mesh;
     long nc = n_cells(), n3 = (long)n * n * n, nq3 = (long)nq * nq * nq, nq2 = (long)nq * nq;
     // elementwise products of the 1D matrices (nq x n)
@@ -991,6 +1002,337 @@ static void assembled_apply(const Laplace<double>& op, const double* src, double
 }
 
 // -------------------------------------------------------------------------------------------
+// Continuous Q_k space on a Cartesian mesh (the continuous levels of cphMG)
+//
+// FE_Q(k) with Gauss-Lobatto support points (the same nodes as FE_DGQ(k)) on the node lattice
+// of a box of N[0] x N[1] x N[2] equal cells: n_d = N_d k + 1 nodes per direction, N_d k when
+// direction d is periodic (the last node plane is the first one).  Nodes are numbered x fastest.
+// Constrained nodes (multigrid/constraints.h:130-197, multigrid_preconditioner_base.cpp:533-545):
+// the nodes on Dirichlet sides, and node 0 when the operator is singular.
+//
+// Operator (OperatorBase::apply, operator_base.cpp:264-310, LaplaceOperator::do_cell_integral,
+// laplace_operator.cpp): cell integrals only, (grad v, grad u) with k+1 Gauss points per
+// direction; constrained entries of src are read as zero and dst = src on constrained nodes
+// (the identity rows of the constrained DoFs).  On equal box cells the integral is the Kronecker
+// sum A = K_x M_y M_z + M_x K_y M_z + M_x M_y K_z of the assembled 1D mass / stiffness
+// matrices, applied as a = M_z x, b = K_z x, c = M_y a, d = K_y a + M_y b, A x = K_x c + M_x d.
+// -------------------------------------------------------------------------------------------
+struct Lattice {
+  int N[3], k;
+  int periodic[3];
+  int dirichlet[6];
+  bool pin_first;
+  int n[3];
+  double h[3];
+  long size() const { return (long)n[0] * n[1] * n[2]; }
+  bool constrained(int gx, int gy, int gz) const {
+    int g[3] = {gx, gy, gz};
+    for (int d = 0; d < 3; ++d)
+      if (!periodic[d] && ((g[d] == 0 && dirichlet[2 * d]) || (g[d] == n[d] - 1 && dirichlet[2 * d + 1])))
+        return true;
+    return pin_first && gx == 0 && gy == 0 && gz == 0;
+  }
+  bool constrained(long i) const {
+    return constrained((int)(i % n[0]), (int)((i / n[0]) % n[1]), (int)(i / ((long)n[0] * n[1])));
+  }
+};
+
+static Lattice make_lattice(const orc_mesh_desc& m, int k, bool singular) {
+  if (m.deform_amp != 0.0) throw std::runtime_error("continuous levels need a Cartesian (affine box) mesh");
+  Lattice L;
+  L.k = k;
+  for (int d = 0; d < 3; ++d) {
+    L.N[d] = m.n_cells[d];
+    L.periodic[d] = m.periodic[d];
+    L.n[d] = m.n_cells[d] * k + (m.periodic[d] ? 0 : 1);
+    L.h[d] = (m.hi[d] - m.lo[d]) / m.n_cells[d];
+  }
+  for (int f = 0; f < 6; ++f) L.dirichlet[f] = (m.bc[f] == 0 && !m.periodic[f / 2]) ? 1 : 0;
+  L.pin_first = singular;
+  return L;
+}
+
+// assembled 1D matrix in band form: row g holds the entries of columns g + o, o = -k..k
+// (column indices wrap on a periodic direction)
+struct Band1D {
+  int n, k;
+  bool periodic;
+  std::vector<double> a;  // [n][2k+1]
+  double at(int g, int o) const { return a[(long)g * (2 * k + 1) + o + k]; }
+  int col(int g, int o) const { return periodic ? ((g + o) % n + n) % n : g + o; }
+};
+
+// element matrices on a cell of length h: mass h (phi_i, phi_j), stiffness (phi_i', phi_j') / h,
+// k+1 Gauss points (exact for both on an affine cell)
+static void element_matrices_1d(int k, double h, std::vector<double>& Me, std::vector<double>& Ke) {
+  std::vector<double> z = gauss_lobatto_points(k + 1), x, w;
+  gauss_rule(k + 1, x, w);
+  Me.assign((k + 1) * (k + 1), 0.0);
+  Ke.assign((k + 1) * (k + 1), 0.0);
+  for (int i = 0; i <= k; ++i)
+    for (int j = 0; j <= k; ++j)
+      for (int q = 0; q <= k; ++q) {
+        Me[i * (k + 1) + j] += h * w[q] * lagrange(z, i, x[q]) * lagrange(z, j, x[q]);
+        Ke[i * (k + 1) + j] += w[q] * lagrange_deriv(z, i, x[q]) * lagrange_deriv(z, j, x[q]) / h;
+      }
+}
+
+static Band1D assemble_1d(const Lattice& L, int d, const std::vector<double>& E) {
+  Band1D B;
+  B.n = L.n[d];
+  B.k = L.k;
+  B.periodic = L.periodic[d];
+  int k = L.k;
+  B.a.assign((long)B.n * (2 * k + 1), 0.0);
+  for (int e = 0; e < L.N[d]; ++e)
+    for (int i = 0; i <= k; ++i) {
+      int gi = e * k + i;
+      if (B.periodic) gi %= B.n;
+      for (int j = 0; j <= k; ++j) B.a[(long)gi * (2 * k + 1) + (j - i) + k] += E[i * (k + 1) + j];
+    }
+  return B;
+}
+
+// out = B along direction dir of a lattice array with extents dims
+template <class Number>
+static void band_apply(const Band1D& B, int dir, const int dims[3], const Number* in, Number* out) {
+  long s[3] = {1, dims[0], (long)dims[0] * dims[1]};
+  long total = (long)dims[0] * dims[1] * dims[2];
+  int k = B.k;
+#pragma omp parallel for
+  for (long i = 0; i < total; ++i) {
+    int g = (int)((i / s[dir]) % dims[dir]);
+    long base = i - (long)g * s[dir];
+    Number acc = 0;
+    for (int o = -k; o <= k; ++o) {
+      double v = B.at(g, o);
+      if (v == 0.0) continue;
+      int c = B.col(g, o);
+      if (c < 0 || c >= B.n) continue;
+      acc += (Number)v * in[base + (long)c * s[dir]];
+    }
+    out[i] = acc;
+  }
+}
+
+template <class Number>
+struct ContinuousLaplace : LevelOp<Number> {
+  Lattice L;
+  Band1D M[3], K[3];
+  long n_dofs() const override { return L.size(); }
+
+  void init(const orc_mesh_desc& m, int degree, bool singular) {
+    L = make_lattice(m, degree, singular);
+    for (int d = 0; d < 3; ++d) {
+      std::vector<double> Me, Ke;
+      element_matrices_1d(degree, L.h[d], Me, Ke);
+      M[d] = assemble_1d(L, d, Me);
+      K[d] = assemble_1d(L, d, Ke);
+    }
+  }
+
+  void apply(const Number* src, Number* dst) const override {
+    long N = L.size();
+    std::vector<Number> x(N), a(N), b(N), c(N), d(N), t(N);
+    for (long i = 0; i < N; ++i) x[i] = L.constrained(i) ? Number(0) : src[i];
+    band_apply(M[2], 2, L.n, x.data(), a.data());
+    band_apply(K[2], 2, L.n, x.data(), b.data());
+    band_apply(M[1], 1, L.n, a.data(), c.data());
+    band_apply(K[1], 1, L.n, a.data(), d.data());
+    band_apply(M[1], 1, L.n, b.data(), t.data());
+    for (long i = 0; i < N; ++i) d[i] += t[i];
+    band_apply(K[0], 0, L.n, c.data(), a.data());
+    band_apply(M[0], 0, L.n, d.data(), b.data());
+    for (long i = 0; i < N; ++i) dst[i] = L.constrained(i) ? src[i] : a[i] + b[i];
+  }
+
+  // sum of the band entries of row g that land on column g (more than o = 0 only when a
+  // periodic direction has a single cell)
+  static double band_diag(const Band1D& B, int g) {
+    double s = 0;
+    for (int o = -B.k; o <= B.k; ++o)
+      if (B.col(g, o) == g) s += B.at(g, o);
+    return s;
+  }
+
+  void diagonal(Number* diag) const override {
+    for (long i = 0; i < L.size(); ++i) {
+      int g[3] = {(int)(i % L.n[0]), (int)((i / L.n[0]) % L.n[1]), (int)(i / ((long)L.n[0] * L.n[1]))};
+      if (L.constrained(g[0], g[1], g[2])) {
+        diag[i] = Number(1);
+        continue;
+      }
+      double m[3], kk[3];
+      for (int d = 0; d < 3; ++d) {
+        m[d] = band_diag(M[d], g[d]);
+        kk[d] = band_diag(K[d], g[d]);
+      }
+      diag[i] = (Number)(kk[0] * m[1] * m[2] + m[0] * kk[1] * m[2] + m[0] * m[1] * kk[2]);
+    }
+  }
+
+  // lattice node of each DG DoF (cell-wise, FE_DGQ nodes x fastest) of the same mesh and degree
+  void dg_map(std::vector<long>& map) const {
+    int k = L.k, n = k + 1;
+    long nc = (long)L.N[0] * L.N[1] * L.N[2];
+    map.resize(nc * n * n * n);
+    for (long c = 0; c < nc; ++c) {
+      int ci[3] = {(int)(c % L.N[0]), (int)((c / L.N[0]) % L.N[1]), (int)(c / ((long)L.N[0] * L.N[1]))};
+      for (int q = 0; q < n * n * n; ++q) {
+        int a[3] = {q % n, (q / n) % n, q / (n * n)};
+        long idx = 0, stride = 1;
+        for (int d = 0; d < 3; ++d) {
+          int g = ci[d] * k + a[d];
+          if (L.periodic[d]) g %= L.n[d];
+          idx += g * stride;
+          stride *= L.n[d];
+        }
+        map[c * n * n * n + q] = idx;
+      }
+    }
+  }
+};
+
+// 1D interpolation between two lattices of one direction (rows: fine nodes; entries: coarse
+// node, value).  p-transfer: same cells, degree kc -> kf; h-transfer: Nf = 2 Nc cells, fine cell
+// ef in coarse cell ef / 2.  A node shared by two cells takes its row from the first cell (the
+// values agree: the basis is interpolatory at the cell ends).
+struct Prol1D {
+  int nf, nc;
+  std::vector<std::vector<std::pair<int, double>>> rows;
+};
+
+static Prol1D lattice_prolongation_1d(int Nc, int kc, int Nf, int kf, bool periodic) {
+  Prol1D P;
+  P.nf = Nf * kf + (periodic ? 0 : 1);
+  P.nc = Nc * kc + (periodic ? 0 : 1);
+  P.rows.assign(P.nf, {});
+  std::vector<char> done(P.nf, 0);
+  std::vector<double> zc = gauss_lobatto_points(kc + 1), zf = gauss_lobatto_points(kf + 1);
+  bool is_h = Nf != Nc;
+  for (int ef = 0; ef < Nf; ++ef)
+    for (int i = 0; i <= kf; ++i) {
+      int g = ef * kf + i;
+      if (periodic) g %= P.nf;
+      if (done[g]) continue;
+      done[g] = 1;
+      int ec = is_h ? ef / 2 : ef;
+      double xi = is_h ? 0.5 * ((ef % 2) + zf[i]) : zf[i];
+      for (int j = 0; j <= kc; ++j) {
+        int cg = ec * kc + j;
+        if (periodic) cg %= P.nc;
+        P.rows[g].push_back({cg, lagrange(zc, j, xi)});
+      }
+    }
+  return P;
+}
+
+// out = P along dir (transpose = false: in has the coarse extent along dir, out the fine one),
+// or P^T (transpose = true: in fine, out coarse)
+template <class Number>
+static void prol_apply(const Prol1D& P, int dir, const int dims_in[3], const Number* in, Number* out,
+                       bool transpose) {
+  int dims_out[3] = {dims_in[0], dims_in[1], dims_in[2]};
+  dims_out[dir] = transpose ? P.nc : P.nf;
+  long si[3] = {1, dims_in[0], (long)dims_in[0] * dims_in[1]};
+  long so[3] = {1, dims_out[0], (long)dims_out[0] * dims_out[1]};
+  long total_out = (long)dims_out[0] * dims_out[1] * dims_out[2];
+  std::fill(out, out + total_out, Number(0));
+  long lines = total_out / dims_out[dir];
+  for (long ln = 0; ln < lines; ++ln) {
+    // base offsets of this line in both arrays
+    long rem = ln, bo = 0, bi = 0;
+    for (int d = 0; d < 3; ++d) {
+      if (d == dir) continue;
+      long c = rem % dims_out[d];
+      rem /= dims_out[d];
+      bo += c * so[d];
+      bi += c * si[d];
+    }
+    for (int g = 0; g < P.nf; ++g)
+      for (auto& e : P.rows[g]) {
+        if (!transpose)
+          out[bo + (long)g * so[dir]] += (Number)e.second * in[bi + (long)e.first * si[dir]];
+        else
+          out[bo + (long)e.first * so[dir]] += (Number)e.second * in[bi + (long)g * si[dir]];
+      }
+  }
+}
+
+template <class Number>
+struct TransferBase {
+  virtual ~TransferBase() {}
+  virtual void prolongate_add(Number* dst, const Number* src) const = 0;
+  virtual void restrict_add(Number* dst, const Number* src) const = 0;
+};
+
+// transfers of the continuous levels (deal.II MGTwoLevelTransfer on FE_Q, a third-party
+// dependency; its published semantics): prolongation interpolates the coarse function, whose
+// constrained nodes are read as zero, and adds it at the unconstrained fine nodes;
+// restriction is the transpose (constrained fine entries ignored, contributions to constrained
+// coarse nodes dropped).  Continuous -> continuous: the interpolation of a tensor-product
+// function is the Kronecker product of the 1D interpolations.  Continuous -> discontinuous (the
+// c-transfer, same mesh and degree): every DG node takes the value of its lattice node.
+template <class Number>
+struct LatticeTransfer : TransferBase<Number> {
+  Lattice Lc, Lf;
+  bool to_dg = false;
+  Prol1D P[3];
+  std::vector<long> map;  // c-transfer: lattice node of each DG DoF
+
+  void setup(const Lattice& coarse, const Lattice* fine_cg, const ContinuousLaplace<Number>* same_mesh) {
+    Lc = coarse;
+    if (!fine_cg) {
+      to_dg = true;
+      same_mesh->dg_map(map);
+      return;
+    }
+    Lf = *fine_cg;
+    for (int d = 0; d < 3; ++d)
+      P[d] = lattice_prolongation_1d(Lc.N[d], Lc.k, Lf.N[d], Lf.k, Lc.periodic[d]);
+  }
+
+  void prolongate_add(Number* dst, const Number* src) const override {
+    long nc = Lc.size();
+    std::vector<Number> u(nc);
+    for (long i = 0; i < nc; ++i) u[i] = Lc.constrained(i) ? Number(0) : src[i];
+    if (to_dg) {
+      for (long i = 0; i < (long)map.size(); ++i) dst[i] += u[map[i]];
+      return;
+    }
+    int d0[3] = {Lc.n[0], Lc.n[1], Lc.n[2]};
+    int d1[3] = {Lf.n[0], Lc.n[1], Lc.n[2]};
+    int d2[3] = {Lf.n[0], Lf.n[1], Lc.n[2]};
+    std::vector<Number> a((long)d1[0] * d1[1] * d1[2]), b((long)d2[0] * d2[1] * d2[2]), c(Lf.size());
+    prol_apply(P[0], 0, d0, u.data(), a.data(), false);
+    prol_apply(P[1], 1, d1, a.data(), b.data(), false);
+    prol_apply(P[2], 2, d2, b.data(), c.data(), false);
+    for (long i = 0; i < Lf.size(); ++i)
+      if (!Lf.constrained(i)) dst[i] += c[i];
+  }
+
+  void restrict_add(Number* dst, const Number* src) const override {
+    long nc = Lc.size();
+    std::vector<Number> v(nc, Number(0));
+    if (to_dg) {
+      for (long i = 0; i < (long)map.size(); ++i) v[map[i]] += src[i];
+    } else {
+      std::vector<Number> w(Lf.size());
+      for (long i = 0; i < Lf.size(); ++i) w[i] = Lf.constrained(i) ? Number(0) : src[i];
+      int d2[3] = {Lf.n[0], Lf.n[1], Lf.n[2]};
+      int d1[3] = {Lf.n[0], Lf.n[1], Lc.n[2]};
+      int d0[3] = {Lf.n[0], Lc.n[1], Lc.n[2]};
+      std::vector<Number> a((long)d1[0] * d1[1] * d1[2]), b((long)d0[0] * d0[1] * d0[2]);
+      prol_apply(P[2], 2, d2, w.data(), a.data(), true);
+      prol_apply(P[1], 1, d1, a.data(), b.data(), true);
+      prol_apply(P[0], 0, d0, b.data(), v.data(), true);
+    }
+    for (long i = 0; i < nc; ++i)
+      if (!Lc.constrained(i)) dst[i] += v[i];
+  }
+};
+
+// -------------------------------------------------------------------------------------------
 // Vectors and Krylov pieces (deal.II SolverCG / ReductionControl semantics)
 // -------------------------------------------------------------------------------------------
 template <class T>
@@ -1136,10 +1478,13 @@ static std::vector<double> tridiag_eigenvalues(std::vector<double> d, std::vecto
 struct LevelInfo {
   int N[3];
   int degree;
+  int dg;  // 1: discontinuous (FE_DGQ), 0: continuous (FE_Q)
 };
 
-static std::vector<LevelInfo> mg_levels(const orc_mesh_desc& fine, int degree, int min_coarse) {
-  // multigrid_preconditioner_base.cpp:97-323 (phMG, PSequenceType::Bisect)
+// multigrid_preconditioner_base.cpp:137-307 (PSequenceType::Bisect): phMG keeps DG on every
+// level; cphMG (c_transfer) puts a continuous level of the finest degree below the DG level
+// (:188-199) and coarsens in the continuous space from there (h-levels at {1, continuous})
+static std::vector<LevelInfo> mg_levels(const orc_mesh_desc& fine, int degree, int min_coarse, bool c_transfer) {
   std::vector<std::array<int, 3>> h;  // coarse to fine
   std::array<int, 3> Nc = {fine.n_cells[0], fine.n_cells[1], fine.n_cells[2]};
   h.push_back(Nc);
@@ -1149,30 +1494,35 @@ static std::vector<LevelInfo> mg_levels(const orc_mesh_desc& fine, int degree, i
     h.push_back(Nc);
   }
   std::reverse(h.begin(), h.end());
-  std::vector<int> p;
+  std::vector<std::pair<int, int>> p;  // (degree, dg), fine to coarse
   int pp = degree;
+  int dg = 1;
+  if (c_transfer) {
+    p.push_back({pp, 1});
+    dg = 0;
+  }
   do {
-    p.push_back(pp);
+    p.push_back({pp, dg});
     pp = std::max(pp / 2, 1);
-  } while (pp != p.back());
+  } while (pp != p.back().first);
   std::reverse(p.begin(), p.end());
   std::vector<LevelInfo> lv;
-  for (size_t i = 0; i + 1 < h.size(); ++i) lv.push_back({{h[i][0], h[i][1], h[i][2]}, p.front()});
-  for (int q : p) lv.push_back({{h.back()[0], h.back()[1], h.back()[2]}, q});
+  for (size_t i = 0; i + 1 < h.size(); ++i) lv.push_back({{h[i][0], h[i][1], h[i][2]}, p.front().first, p.front().second});
+  for (auto q : p) lv.push_back({{h.back()[0], h.back()[1], h.back()[2]}, q.first, q.second});
   return lv;
 }
 
 template <class Number>
 struct Chebyshev {
   // deal.II PreconditionChebyshev (first kind), chebyshev_smoother.h:79-210
-  const Laplace<Number>* A;
+  const LevelOp<Number>* A;
   std::vector<Number> inv_diag;
   int degree;
   double theta, delta, lambda_max, lambda_min;
   int eig_its;
   mutable std::vector<Number> t1, t2, old;
 
-  void setup(const Laplace<Number>* op, int deg, double range, int eig_iters) {
+  void setup(const LevelOp<Number>* op, int deg, double range, int eig_iters) {
     A = op;
     degree = deg;
     long N = op->n_dofs();
@@ -1264,7 +1614,7 @@ static std::vector<double> h_prolongation(int k, int child) {
 }
 
 template <class Number>
-struct Transfer {
+struct Transfer : TransferBase<Number> {
   // MGTwoLevelTransfer for DG (element-local interpolation; restriction = transpose)
   bool is_h;
   int Nf[3], Nc[3], nf, nc;
@@ -1288,7 +1638,7 @@ struct Transfer {
     }
   }
   // dst_fine += P src_coarse
-  void prolongate_add(Number* dst, const Number* src) const {
+  void prolongate_add(Number* dst, const Number* src) const override {
     long ncells_f = (long)Nf[0] * Nf[1] * Nf[2];
     long nf3 = (long)nf * nf * nf, nc3 = (long)nc * nc * nc;
 #pragma omp parallel
@@ -1314,7 +1664,7 @@ struct Transfer {
     }
   }
   // dst_coarse += P^T src_fine
-  void restrict_add(Number* dst, const Number* src) const {
+  void restrict_add(Number* dst, const Number* src) const override {
     long ncells_c = (long)Nc[0] * Nc[1] * Nc[2];
     long nf3 = (long)nf * nf * nf, nc3 = (long)nc * nc * nc;
 #pragma omp parallel
@@ -1349,11 +1699,10 @@ struct Transfer {
 template <class Number>
 struct Multigrid {
   std::vector<LevelInfo> info;
-  std::vector<std::shared_ptr<Geometry>> geos;
-  std::vector<std::unique_ptr<Laplace<Number>>> ops;
+  std::vector<std::unique_ptr<LevelOp<Number>>> ops;
   std::vector<std::unique_ptr<Chebyshev<Number>>> smoothers;
-  std::vector<Transfer<Number>> transfers;  // transfers[l] between l-1 and l
-  std::unique_ptr<Laplace<double>> coarse_op_d;  // coarse operator in double (optional)
+  std::vector<std::unique_ptr<TransferBase<Number>>> transfers;  // transfers[l] between l-1 and l
+  std::unique_ptr<LevelOp<double>> coarse_op_d;  // coarse operator in double (optional)
   std::vector<double> coarse_inv_diag_d;
   std::vector<Number> coarse_inv_diag;
   mutable std::vector<std::vector<Number>> defect, solution, t;
@@ -1361,9 +1710,23 @@ struct Multigrid {
   orc_solver_desc desc;
   mutable long coarse_its = 0, vcycles = 0;
 
+  // operator of level l in precision T: SIPG on DG levels, the lattice operator on continuous ones
+  template <class T>
+  static std::unique_ptr<LevelOp<T>> make_op(const orc_mesh_desc& md, const LevelInfo& li, double ip, bool singular) {
+    if (li.dg) {
+      auto g = make_geometry(make_mesh(md), li.degree + 1);
+      auto* op = new Laplace<T>();
+      op->init(g, li.degree, ip);
+      return std::unique_ptr<LevelOp<T>>(op);
+    }
+    auto* op = new ContinuousLaplace<T>();
+    op->init(md, li.degree, singular);
+    return std::unique_ptr<LevelOp<T>>(op);
+  }
+
   void setup(const orc_mesh_desc& fine, int degree, double ip, const orc_solver_desc& d) {
     desc = d;
-    info = mg_levels(fine, degree, std::max(1, d.min_coarse_cells));
+    info = mg_levels(fine, degree, std::max(1, d.min_coarse_cells), d.mg_type == 1);
     int L = (int)info.size();
     ops.resize(L);
     smoothers.resize(L);
@@ -1371,14 +1734,10 @@ struct Multigrid {
     defect.resize(L);
     solution.resize(L);
     t.resize(L);
-    std::shared_ptr<Geometry> last;
     for (int l = 0; l < L; ++l) {
       orc_mesh_desc md = fine;
       for (int e = 0; e < 3; ++e) md.n_cells[e] = info[l].N[e];
-      Mesh m = make_mesh(md);
-      auto g = make_geometry(m, info[l].degree + 1);
-      ops[l].reset(new Laplace<Number>());
-      ops[l]->init(g, info[l].degree, ip);
+      ops[l] = make_op<Number>(md, info[l], ip, d.singular != 0);
       long N = ops[l]->n_dofs();
       defect[l].assign(N, Number(0));
       solution[l].assign(N, Number(0));
@@ -1386,7 +1745,24 @@ struct Multigrid {
       if (l > 0) {
         smoothers[l].reset(new Chebyshev<Number>());
         smoothers[l]->setup(ops[l].get(), d.cheb_degree, d.smoothing_range, d.eig_iters);
-        transfers[l].setup(info[l - 1], info[l]);
+        const LevelInfo &ci = info[l - 1], &fi = info[l];
+        if (ci.dg) {
+          auto* tr = new Transfer<Number>();
+          tr->setup(ci, fi);
+          transfers[l].reset(tr);
+        } else {
+          orc_mesh_desc mc = fine;
+          for (int e = 0; e < 3; ++e) mc.n_cells[e] = ci.N[e];
+          Lattice lc = make_lattice(mc, ci.degree, d.singular != 0);
+          auto* tr = new LatticeTransfer<Number>();
+          if (fi.dg) {
+            tr->setup(lc, nullptr, (const ContinuousLaplace<Number>*)ops[l - 1].get());
+          } else {
+            Lattice lf = make_lattice(md, fi.degree, d.singular != 0);
+            tr->setup(lc, &lf, nullptr);
+          }
+          transfers[l].reset(tr);
+        }
       }
       if (l == 0) {
         std::vector<Number> dg(N);
@@ -1394,8 +1770,7 @@ struct Multigrid {
         coarse_inv_diag.resize(N);
         for (long i = 0; i < N; ++i) coarse_inv_diag[i] = std::fabs((double)dg[i]) > 1e-10 ? Number(1) / dg[i] : Number(1);
         if (d.coarse_double) {
-          coarse_op_d.reset(new Laplace<double>());
-          coarse_op_d->init(g, info[0].degree, ip);
+          coarse_op_d = make_op<double>(md, info[0], ip, d.singular != 0);
           std::vector<double> dd(N);
           coarse_op_d->diagonal(dd.data());
           coarse_inv_diag_d.resize(N);
@@ -1452,9 +1827,9 @@ struct Multigrid {
     ops[l]->apply(solution[l].data(), t[l].data());
     long N = (long)t[l].size();
     for (long i = 0; i < N; ++i) t[l][i] = defect[l][i] - t[l][i];
-    transfers[l].restrict_add(defect[l - 1].data(), t[l].data());
+    transfers[l]->restrict_add(defect[l - 1].data(), t[l].data());
     v_cycle(l - 1);
-    transfers[l].prolongate_add(solution[l].data(), solution[l - 1].data());
+    transfers[l]->prolongate_add(solution[l].data(), solution[l - 1].data());
     smoothers[l]->iterate(solution[l], defect[l], false);
   }
 
@@ -1632,6 +2007,7 @@ void orc_default_solver_desc(orc_solver_desc* d) {
   d->coarse_double = 0;
   d->min_coarse_cells = 2;
   d->singular = 0;
+  d->mg_type = 0;
 }
 
 // multigrid handle (templated on the V-cycle precision)
@@ -1766,13 +2142,64 @@ void orc_chebyshev(void* h, int degree, double range, int eig_iters, int mode, c
 
 // transfers between two levels (coarse degree/cells -> fine)
 void orc_transfer(int kc, int kf, const int* Nc, const int* Nf, int restrict_mode, const double* src, double* dst) {
-  LevelInfo c{{Nc[0], Nc[1], Nc[2]}, kc}, f{{Nf[0], Nf[1], Nf[2]}, kf};
+  LevelInfo c{{Nc[0], Nc[1], Nc[2]}, kc, 1}, f{{Nf[0], Nf[1], Nf[2]}, kf, 1};
   Transfer<double> t;
   t.setup(c, f);
   if (restrict_mode)
     t.restrict_add(dst, src);
   else
     t.prolongate_add(dst, src);
+}
+
+// continuous levels: the lattice operator (cphMG) and its transfers
+struct CGHandle {
+  ContinuousLaplace<double> d;
+  ContinuousLaplace<float> f;
+};
+void* orc_cg_create(const orc_mesh_desc* m, int degree, int singular) {
+  auto* h = new CGHandle();
+  h->d.init(*m, degree, singular != 0);
+  h->f.init(*m, degree, singular != 0);
+  return h;
+}
+void orc_cg_destroy(void* h) { delete (CGHandle*)h; }
+long orc_cg_n_dofs(void* h) { return ((CGHandle*)h)->d.n_dofs(); }
+void orc_cg_apply_f64(void* h, const double* src, double* dst) { ((CGHandle*)h)->d.apply(src, dst); }
+void orc_cg_apply_f32(void* h, const float* src, float* dst) { ((CGHandle*)h)->f.apply(src, dst); }
+void orc_cg_diagonal_f64(void* h, double* d) { ((CGHandle*)h)->d.diagonal(d); }
+void orc_cg_constrained(void* h, unsigned char* mask) {
+  const Lattice& L = ((CGHandle*)h)->d.L;
+  for (long i = 0; i < L.size(); ++i) mask[i] = L.constrained(i) ? 1 : 0;
+}
+void orc_cg_dg_map(void* h, long* map) {
+  std::vector<long> m;
+  ((CGHandle*)h)->d.dg_map(m);
+  std::copy(m.begin(), m.end(), map);
+}
+// transfer from the continuous level (Nc cells, degree kc) to the level of mesh m (degree kf,
+// discontinuous when fine_dg, then with Nc = m's cells and kc = kf)
+void orc_lattice_transfer(const orc_mesh_desc* m, const int* Nc, int kc, int kf, int fine_dg, int singular,
+                          int restrict_mode, const double* src, double* dst) {
+  orc_mesh_desc mc = *m;
+  for (int e = 0; e < 3; ++e) mc.n_cells[e] = Nc[e];
+  Lattice lc = make_lattice(mc, kc, singular != 0);
+  LatticeTransfer<double> t;
+  ContinuousLaplace<double> same;
+  if (fine_dg) {
+    same.init(mc, kc, singular != 0);
+    t.setup(lc, nullptr, &same);
+  } else {
+    Lattice lf = make_lattice(*m, kf, singular != 0);
+    t.setup(lc, &lf, nullptr);
+  }
+  if (restrict_mode)
+    t.restrict_add(dst, src);
+  else
+    t.prolongate_add(dst, src);
+}
+int orc_mg_level_dg(void* mg, int l) {
+  auto* m = (MGHandle*)mg;
+  return m->is_float ? m->mf->info[l].dg : m->md->info[l].dg;
 }
 
 // 1D finite element data, so the tests can check the product's tables

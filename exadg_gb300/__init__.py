@@ -31,6 +31,8 @@ EXG_ERR_NEEDS_UPDATE = 6
 PREC_F64 = 0
 PREC_F32 = 1
 PREC_F64E = 2
+MG_PH = 0  # phMG: DG on every level
+MG_CPH = 1  # cphMG: continuous levels below the finest DG level
 
 BC_DIRICHLET = 0
 BC_NEUMANN = 1
@@ -71,6 +73,7 @@ class MGDesc(ctypes.Structure):
         ("singular", ctypes.c_int),
         ("use_graph", ctypes.c_int),
         ("fuse_smoother", ctypes.c_int),
+        ("mg_type", ctypes.c_int),
     ]
 
 
@@ -83,6 +86,7 @@ class MGInfo(ctypes.Structure):
         ("eig_iters", ctypes.c_int * 32),
         ("coarse_iterations", ctypes.c_longlong),
         ("vcycles", ctypes.c_longlong),
+        ("dg", ctypes.c_int * 32),
     ]
 
 
@@ -110,7 +114,8 @@ class CGResult(ctypes.Structure):
 
 # every symbol declared in include/exadg_gb300.h
 EXPORTED_SYMBOLS = [
-    "exg_mesh_create", "exg_mesh_destroy", "exg_sipg_create", "exg_sipg_destroy", "exg_sipg_n_dofs",
+    "exg_mesh_create", "exg_mesh_destroy", "exg_sipg_create", "exg_continuous_create", "exg_sipg_destroy",
+    "exg_sipg_n_dofs",
     "exg_sipg_info", "exg_sipg_tune", "exg_sipg_set_launch_config", "exg_sipg_apply_f64", "exg_sipg_apply_f32",
     "exg_sipg_residual_f64", "exg_sipg_apply_host_f64", "exg_sipg_inverse_diagonal_f64",
     "exg_sipg_inverse_diagonal_f32", "exg_sipg_quadrature_points", "exg_sipg_rhs", "exg_mg_default_desc",
@@ -141,6 +146,7 @@ def load_library(path=LIB_PATH):
         "exg_mesh_create": [ctypes.POINTER(MeshDesc), PP],
         "exg_mesh_destroy": [P],
         "exg_sipg_create": [P, I, D, I, PP],
+        "exg_continuous_create": [P, I, I, I, PP],
         "exg_sipg_destroy": [P],
         "exg_sipg_n_dofs": [P, ctypes.POINTER(LL)],
         "exg_sipg_info": [P, ctypes.POINTER(I), ctypes.POINTER(I), ctypes.POINTER(I)],
@@ -279,12 +285,16 @@ class Mesh:
 class LaplaceOperator:
     """SIPG Laplace operator (Poisson::LaplaceOperator) on FE_DGQ(degree), QGauss(degree+1)."""
 
-    def __init__(self, mesh, degree, ip_factor=1.0, precision=PREC_F64):
+    def __init__(self, mesh, degree, ip_factor=1.0, precision=PREC_F64, _continuous_singular=None):
         self.mesh = mesh
         self.degree = degree
         self.precision = precision
         h = ctypes.c_void_p()
-        _check(load_library().exg_sipg_create(mesh.h, degree, ip_factor, precision, ctypes.byref(h)))
+        if _continuous_singular is None:
+            _check(load_library().exg_sipg_create(mesh.h, degree, ip_factor, precision, ctypes.byref(h)))
+        else:
+            _check(load_library().exg_continuous_create(mesh.h, degree, precision, int(_continuous_singular),
+                                                        ctypes.byref(h)))
         self.h = h
         n = ctypes.c_longlong()
         _check(_lib.exg_sipg_n_dofs(h, ctypes.byref(n)))
@@ -386,12 +396,25 @@ class LaplaceOperator:
         return b
 
 
+class ContinuousLaplaceOperator(LaplaceOperator):
+    """Continuous Laplace operator on FE_Q(degree) of a Cartesian mesh, as on the continuous
+    levels of cphMG (LaplaceOperator with a continuous DoFHandler): DoFs are the lattice nodes
+    (N_d * degree + 1 per direction, N_d * degree when periodic, x fastest); constrained DoFs
+    (Dirichlet sides, DoF 0 when singular) keep dst = src."""
+
+    def __init__(self, mesh, degree, precision=PREC_F64, singular=False):
+        super().__init__(mesh, degree, 1.0, precision, _continuous_singular=bool(singular))
+
+
 class MultigridPreconditioner:
-    """phMG V-cycle preconditioner (MultigridPreconditionerBase::vmult)."""
+    """phMG / cphMG V-cycle preconditioner (MultigridPreconditionerBase::vmult).
+
+    mg_type: MG_PH (DG on every level) or MG_CPH (continuous FE_Q levels below the finest DG
+    level, the reference's default for the sine and Taylor-Green applications; Cartesian meshes)."""
 
     def __init__(self, operator, mg_precision=PREC_F32, cheb_degree=5, smoothing_range=20.0, eig_iters=20,
                  coarse_rel_tol=1e-3, coarse_abs_tol=1e-12, coarse_max_iter=10000, coarse_double=False,
-                 min_coarse_cells=2, singular=False, use_graph=True, fuse_smoother=True):
+                 min_coarse_cells=2, singular=False, use_graph=True, fuse_smoother=True, mg_type=0):
         d = MGDesc()
         _check(load_library().exg_mg_default_desc(ctypes.byref(d)))
         d.mg_precision = mg_precision
@@ -406,6 +429,7 @@ class MultigridPreconditioner:
         d.singular = int(singular)
         d.use_graph = int(use_graph)
         d.fuse_smoother = int(fuse_smoother)
+        d.mg_type = int(mg_type)
         self.desc = d
         self.operator = operator
         h = ctypes.c_void_p()
@@ -443,7 +467,7 @@ class MultigridPreconditioner:
         return dict(
             n_levels=i.n_levels,
             levels=[dict(degree=i.degree[l], n_cells=tuple(i.n_cells[l]), lambda_max=i.lambda_max[l],
-                         eig_iters=i.eig_iters[l]) for l in range(i.n_levels)],
+                         eig_iters=i.eig_iters[l], dg=bool(i.dg[l])) for l in range(i.n_levels)],
             coarse_iterations=i.coarse_iterations,
             vcycles=i.vcycles,
         )

@@ -31,6 +31,7 @@ SOURCES = [
     "capi.cpp",
     "noalloc.cu",
     "cnn.cu",
+    "lattice.cu",
 ]
 
 

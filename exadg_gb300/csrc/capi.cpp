@@ -74,6 +74,13 @@ exg_status exg_sipg_create(const exg_mesh* mesh, int degree, double ip_factor, i
   EXG_API_END
 }
 
+exg_status exg_continuous_create(const exg_mesh* mesh, int degree, int precision, int singular, exg_op** op) {
+  EXG_API_BEGIN
+  EXG_CHECK(mesh && op, EXG_ERR_INVALID, "null argument");
+  *op = exg_op::continuous_level(mesh->info, degree, precision, singular != 0).release();
+  EXG_API_END
+}
+
 exg_status exg_sipg_destroy(exg_op* op) {
   EXG_API_BEGIN
   delete op;
@@ -215,6 +222,7 @@ exg_status exg_mg_default_desc(exg_mg_desc* d) {
   d->singular = 0;
   d->use_graph = 1;
   d->fuse_smoother = 1;
+  d->mg_type = EXG_MG_PH;
   EXG_API_END
 }
 

@@ -67,8 +67,27 @@ exg_op::exg_op(const MeshInfo& m, int deg, double ip_factor, int prec)
   }
 }
 
+std::unique_ptr<exg_op> exg_op::continuous_level(const MeshInfo& m, int deg, int prec, bool singular) {
+  EXG_CHECK(prec == EXG_PREC_F32 || prec == EXG_PREC_F64, EXG_ERR_UNSUPPORTED,
+            "continuous levels compute in FP32 or FP64");
+  std::unique_ptr<exg_op> op(new exg_op(m, deg, 1.0, prec));
+  op->continuous = true;
+  op->lat.reset(new LatticeHost());
+  make_lattice(m, deg, singular, *op->lat);
+  lattice_prepare(*op->lat, prec);
+  return op;
+}
+
 void exg_op::apply(const void* src, void* dst, int n_rhs, cudaStream_t s, const exg::PointEpilogue& ep,
                    long long cell_begin, long long cell_end) const {
+  if (continuous) {
+    EXG_CHECK(cell_begin == 0 && cell_end < 0, EXG_ERR_INVALID, "continuous levels apply on the whole lattice");
+    EXG_CHECK(n_rhs == 1 || ep.mode < 0, EXG_ERR_INVALID, "fused store needs a single right-hand side");
+    const size_t stride = (size_t)lat->size() * (precision == EXG_PREC_F32 ? 4 : 8);
+    for (int r = 0; r < n_rhs; ++r)
+      lattice_apply(*lat, precision, (const char*)src + r * stride, dst ? (char*)dst + r * stride : nullptr, s, ep);
+    return;
+  }
   const long long nc = mesh.n_cells();
   if (cell_end < 0) cell_end = nc;
   EXG_CHECK(cell_begin >= 0 && cell_begin < cell_end && cell_end <= nc, EXG_ERR_INVALID, "bad cell range");
@@ -102,6 +121,7 @@ HostPipe::~HostPipe() {
 // copied out on a third, so the host-to-device copy of slab j+1, the apply of slab j and the copy
 // back of slab j-1 overlap.  With periodicity in z, slab 0 needs slab K-1 and is applied last.
 void exg_op::apply_host(const double* src_host, double* dst_host, int n_slabs, cudaStream_t s) {
+  EXG_CHECK(!continuous, EXG_ERR_UNSUPPORTED, "not available for a continuous operator");
   EXG_CHECK(precision != EXG_PREC_F32, EXG_ERR_INVALID, "host apply needs an FP64-storage operator");
   const int Nz = mesh.N[2];
   const int K = std::max(1, std::min(n_slabs, Nz));
@@ -156,7 +176,9 @@ void exg_op::apply_host(const double* src_host, double* dst_host, int n_slabs, c
 }
 
 void exg_op::diagonal(void* d, bool invert, cudaStream_t s) const {
-  if (cartesian)
+  if (continuous)
+    lattice_diagonal(*lat, precision, d, invert, s);
+  else if (cartesian)
     cart_diagonal(cart, precision, d, invert, s);
   else
     general_diagonal(*geo, fe, d, invert, s);
@@ -166,7 +188,7 @@ void exg_op::diagonal(void* d, bool invert, cudaStream_t s) const {
 // degree and precision (CUDA events, median of 5 launches after 2 warm-up launches) and keep the
 // fastest.  Curved meshes have a single variant.
 int exg_op::tune(int n_rhs, cudaStream_t s, std::vector<std::pair<int, float>>* timings) {
-  if (!cartesian) return 0;
+  if (!cartesian || continuous) return 0;
   std::vector<int> opts = cart_cpb_options(n, precision);
   size_t bytes = (size_t)n_dofs() * n_rhs * (precision == EXG_PREC_F32 ? 4 : 8);
   void* x = dalloc(bytes);
@@ -231,6 +253,7 @@ CGWorkspace::~CGWorkspace() {
 }
 
 void exg_op::ensure_rhs_geometry(cudaStream_t s) {
+  EXG_CHECK(!continuous, EXG_ERR_UNSUPPORTED, "not available for a continuous operator");
   if (rhs_geo) return;
   rhs_geo.reset(new GeneralGeom());
   rhs_geo->build(mesh, fe, ip, EXG_PREC_F64, true, s);
@@ -359,7 +382,16 @@ static std::vector<double> tridiag_eigs(std::vector<double> d, std::vector<doubl
 }
 
 // MGLevelInfo list for phMG with the Bisect p-sequence (multigrid_preconditioner_base.cpp:97-323)
-static std::vector<std::pair<std::array<int, 3>, int>> mg_level_list(const int Nf[3], int degree, int min_coarse) {
+struct LevelSpec {
+  std::array<int, 3> N;
+  int degree;
+  int dg;
+};
+
+// multigrid_preconditioner_base.cpp:137-307 with PSequenceType::Bisect: h-levels at the coarsest
+// p-level, then the p-levels on the finest mesh.  cphMG (c_transfer) inserts a continuous level of
+// the finest degree below the DG level (:188-199); every level below it is continuous.
+static std::vector<LevelSpec> mg_level_list(const int Nf[3], int degree, int min_coarse, bool c_transfer) {
   std::vector<std::array<int, 3>> h;
   std::array<int, 3> Nc = {Nf[0], Nf[1], Nf[2]};
   h.push_back(Nc);
@@ -369,16 +401,20 @@ static std::vector<std::pair<std::array<int, 3>, int>> mg_level_list(const int N
     h.push_back(Nc);
   }
   std::reverse(h.begin(), h.end());
-  std::vector<int> p;
-  int pp = degree;
+  std::vector<std::pair<int, int>> p;  // (degree, dg), fine to coarse
+  int pp = degree, dg = 1;
+  if (c_transfer) {
+    p.push_back({pp, 1});
+    dg = 0;
+  }
   do {
-    p.push_back(pp);
+    p.push_back({pp, dg});
     pp = std::max(pp / 2, 1);
-  } while (pp != p.back());
+  } while (pp != p.back().first);
   std::reverse(p.begin(), p.end());
-  std::vector<std::pair<std::array<int, 3>, int>> out;
-  for (size_t i = 0; i + 1 < h.size(); ++i) out.push_back({h[i], p.front()});
-  for (int q : p) out.push_back({h.back(), q});
+  std::vector<LevelSpec> out;
+  for (size_t i = 0; i + 1 < h.size(); ++i) out.push_back({h[i], p.front().first, p.front().second});
+  for (auto q : p) out.push_back({h.back(), q.first, q.second});
   return out;
 }
 }  // namespace exg
@@ -453,26 +489,34 @@ static TransferParams make_transfer(const MGLevel& c, const MGLevel& f) {
 }
 
 exg_mg::exg_mg(const exg_op& fine, const exg_mg_desc& d) : desc(d) {
+  EXG_CHECK(!fine.continuous, EXG_ERR_UNSUPPORTED, "the multigrid's fine operator is the DG operator");
   EXG_CHECK(d.mg_precision == EXG_PREC_F32 || d.mg_precision == EXG_PREC_F64, EXG_ERR_INVALID,
             "mg_precision must be EXG_PREC_F32 or EXG_PREC_F64");
   EXG_CHECK(d.cheb_degree >= 1 && d.eig_iters >= 1, EXG_ERR_INVALID, "bad smoother parameters");
   prec = d.mg_precision;
   coarse_prec = d.coarse_double ? EXG_PREC_F64 : prec;
-  auto list = mg_level_list(fine.mesh.N, fine.degree, std::max(1, d.min_coarse_cells));
+  EXG_CHECK(d.mg_type == EXG_MG_PH || d.mg_type == EXG_MG_CPH, EXG_ERR_INVALID, "mg_type must be EXG_MG_PH or EXG_MG_CPH");
+  EXG_CHECK(d.mg_type == EXG_MG_PH || fine.cartesian, EXG_ERR_UNSUPPORTED,
+            "cphMG (continuous levels) needs a Cartesian mesh");
+  auto list = mg_level_list(fine.mesh.N, fine.degree, std::max(1, d.min_coarse_cells), d.mg_type == EXG_MG_CPH);
   EXG_CHECK(list.size() <= 32, EXG_ERR_UNSUPPORTED, "too many levels");
   cudaStream_t s = nullptr;
   lv.resize(list.size());
   for (size_t l = 0; l < list.size(); ++l) {
     MGLevel& L = lv[l];
-    for (int e = 0; e < 3; ++e) L.N[e] = list[l].first[e];
-    L.degree = list[l].second;
+    for (int e = 0; e < 3; ++e) L.N[e] = list[l].N[e];
+    L.degree = list[l].degree;
+    L.dg = list[l].dg;
     MeshInfo m = fine.mesh;
     for (int e = 0; e < 3; ++e) {
       m.d.n_cells[e] = L.N[e];
       m.N[e] = L.N[e];
       m.h[e] = (m.d.hi[e] - m.d.lo[e]) / L.N[e];
     }
-    L.op.reset(new exg_op(m, L.degree, fine.ip, prec));
+    if (L.dg)
+      L.op.reset(new exg_op(m, L.degree, fine.ip, prec));
+    else
+      L.op = exg_op::continuous_level(m, L.degree, prec, d.singular != 0);
     L.n = L.op->n_dofs();
     if (L.op->cartesian && l > 0) L.op->tune(1, s, nullptr);  // autotuned launch variant per level
     size_t bytes = L.n * psize(prec);
@@ -490,12 +534,24 @@ exg_mg::exg_mg(const exg_op& fine, const exg_mg_desc& d) : desc(d) {
         level_eigen<float>(L, d, s);
       else
         level_eigen<double>(L, d, s);
-      L.tr = make_transfer(lv[l - 1], L);
+      MGLevel& C = lv[l - 1];
+      if (C.dg) {
+        L.tr = make_transfer(C, L);
+      } else {
+        L.ltr.reset(new LatticeTransfer());
+        if (L.dg)
+          L.ltr->setup_dg(*C.op->lat, prec);
+        else
+          L.ltr->setup(*C.op->lat, *L.op->lat, prec);
+      }
     } else {
       n_coarse = (int)L.n;
       EXG_CHECK(L.n <= 4096, EXG_ERR_UNSUPPORTED, "coarse level too large for the single-CTA coarse solver");
       MeshInfo mc = m;
-      coarse_op.reset(new exg_op(mc, L.degree, fine.ip, coarse_prec));
+      if (L.dg)
+        coarse_op.reset(new exg_op(mc, L.degree, fine.ip, coarse_prec));
+      else
+        coarse_op = exg_op::continuous_level(mc, L.degree, coarse_prec, d.singular != 0);
       size_t cb = psize(coarse_prec);
       coarseA = dalloc((size_t)L.n * L.n * cb);
       void* eye = dalloc((size_t)L.n * L.n * cb);
@@ -622,14 +678,18 @@ void exg_mg::v_cycle(int l, cudaStream_t s) {
     else
       rsub<double>((const double*)L.def, (double*)L.t, L.n, s);
   }
-  if (prec == EXG_PREC_F32)
+  if (L.ltr)
+    L.ltr->restrict_add(L.t, C.def, s);
+  else if (prec == EXG_PREC_F32)
     restrict_add<float>(L.tr, (const float*)L.t, (float*)C.def, s);
   else
     restrict_add<double>(L.tr, (const double*)L.t, (double*)C.def, s);
   mark(1);
   v_cycle(l - 1, s);
   mark(2);
-  if (prec == EXG_PREC_F32)
+  if (L.ltr)
+    L.ltr->prolongate_add(C.sol, L.sol, s);
+  else if (prec == EXG_PREC_F32)
     prolongate_add<float>(L.tr, (const float*)C.sol, (float*)L.sol, s);
   else
     prolongate_add<double>(L.tr, (const double*)C.sol, (double*)L.sol, s);
@@ -712,6 +772,7 @@ void exg_mg::info(exg_mg_info& out) const {
     for (int e = 0; e < 3; ++e) out.n_cells[l][e] = lv[l].N[e];
     out.lambda_max[l] = lv[l].lambda_max;
     out.eig_iters[l] = lv[l].eig_its;
+    out.dg[l] = lv[l].dg;
   }
   long long its = 0;
   if (its_dev) cudaMemcpy(&its, its_dev, sizeof(long long), cudaMemcpyDeviceToHost);

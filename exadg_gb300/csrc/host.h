@@ -7,6 +7,7 @@
 #include "cg_device.h"
 #include "general.h"
 #include "internal.h"
+#include "lattice.h"
 #include "solver_kernels.h"
 
 struct exg_mesh {
@@ -61,7 +62,11 @@ struct exg_op {
   std::unique_ptr<exg::GeneralGeom> rhs_geo;  // FP64 geometry with points (rhs / quadrature points)
 
   exg_op(const exg::MeshInfo& m, int degree, double ip, int precision);
-  long long n_dofs() const { return mesh.n_cells() * n * n * n; }
+  // continuous FE_Q(degree) Laplacian on the node lattice (a cphMG level; Cartesian meshes)
+  static std::unique_ptr<exg_op> continuous_level(const exg::MeshInfo& m, int degree, int precision, bool singular);
+  bool continuous = false;
+  std::unique_ptr<exg::LatticeHost> lat;
+  long long n_dofs() const { return continuous ? lat->size() : mesh.n_cells() * n * n * n; }
   // dst = A src on the cells [cell_begin, cell_end) (cell_end < 0: all cells)
   void apply(const void* src, void* dst, int n_rhs, cudaStream_t s,
              const exg::PointEpilogue& ep = exg::PointEpilogue(), long long cell_begin = 0,
@@ -82,6 +87,7 @@ namespace exg {
 struct MGLevel {
   int N[3];
   int degree;
+  int dg = 1;  // 0: continuous level (cphMG)
   std::unique_ptr<exg_op> op;
   long long n = 0;
   void* invd = nullptr;
@@ -92,7 +98,8 @@ struct MGLevel {
   void* old = nullptr;
   double theta = 1, delta = 0, lambda_max = 0, lambda_min = 0;
   int eig_its = 0;
-  TransferParams tr{};  // transfer from level l-1 to l
+  TransferParams tr{};  // transfer from level l-1 to l (l-1 discontinuous)
+  std::unique_ptr<LatticeTransfer> ltr;  // transfer from a continuous level l-1
 };
 }  // namespace exg
 

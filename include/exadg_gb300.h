@@ -65,6 +65,16 @@ exg_status exg_mesh_destroy(exg_mesh* mesh);
  * (Poisson::LaplaceOperator::initialize, poisson/spatial_discretization/laplace_operator.cpp:33-51;
  *  penalty IP::calculate_penalty_parameter, operators/interior_penalty_parameter.h:45-97). */
 exg_status exg_sipg_create(const exg_mesh* mesh, int degree, double ip_factor, int precision, exg_op** op);
+/* Continuous Laplace operator on FE_Q(degree) (Gauss-Lobatto support points) of a Cartesian
+ * mesh, as on the continuous levels of cphMG: cell integrals with QGauss(degree+1), constrained
+ * DoFs (Dirichlet sides; DoF 0 when singular != 0) keep dst = src
+ * (LaplaceOperator with a continuous DoFHandler, laplace_operator.cpp:387-436;
+ *  OperatorBase::apply, operators/operator_base.cpp:264-310; multigrid/constraints.h:130-197).
+ * DoFs are the nodes of the lattice of N_d * degree + 1 points per direction (N_d * degree when
+ * periodic), x fastest.  precision: EXG_PREC_F64 or EXG_PREC_F32.  The handle works with
+ * exg_sipg_apply_f64/_f32, exg_sipg_residual_f64, exg_sipg_inverse_diagonal_f64/_f32,
+ * exg_sipg_n_dofs, exg_sipg_destroy and exg_cg_solve (without multigrid). */
+exg_status exg_continuous_create(const exg_mesh* mesh, int degree, int precision, int singular, exg_op** op);
 exg_status exg_sipg_destroy(exg_op* op);
 exg_status exg_sipg_n_dofs(const exg_op* op, long long* n_dofs);
 exg_status exg_sipg_info(const exg_op* op, int* degree, int* precision, int* cartesian);
@@ -133,7 +143,15 @@ typedef struct {
   int fuse_smoother;       /* 1: Chebyshev steps and the level residual are computed in the operator
                             * kernels' store (deal.II's pre/post-loop operations of a Chebyshev
                             * vmult); 0: separate vector kernels.  Both give the same iterates. */
+  int mg_type;             /* EXG_MG_PH (0): DG on every level (phMG); EXG_MG_CPH (1): cphMG, a
+                            * continuous FE_Q(k) level below the finest DG level and coarsening in
+                            * the continuous space (multigrid_preconditioner_base.cpp:188-199;
+                            * the default of applications/poisson/sine/application.h:167).
+                            * Continuous levels need a Cartesian mesh. */
 } exg_mg_desc;
+
+#define EXG_MG_PH 0
+#define EXG_MG_CPH 1
 
 typedef struct {
   int n_levels;
@@ -143,9 +161,10 @@ typedef struct {
   int eig_iters[32];
   long long coarse_iterations;  /* accumulated coarse CG iterations */
   long long vcycles;
+  int dg[32];              /* 1: discontinuous level, 0: continuous level (cphMG) */
 } exg_mg_info;
 
-/* phMG (Bisect p-sequence, DG) with Chebyshev-Jacobi smoothing and a coarse CG
+/* phMG or cphMG (Bisect p-sequence) with Chebyshev-Jacobi smoothing and a coarse CG
  * (MultigridPreconditionerBase::initialize/vmult, multigrid/multigrid_preconditioner_base.cpp:55-95,
  *  673-683; MultigridAlgorithm::v_cycle, multigrid/multigrid_algorithm.h:172-240). */
 exg_status exg_mg_default_desc(exg_mg_desc* desc);

@@ -440,7 +440,19 @@ def run_solve(args):
                         "mixed": {kk: rm[kk] for kk in ("iterations", "wall_seconds", "setup_seconds", "rn", "r0")},
                         "speedup": r64["wall_seconds"] / rm["wall_seconds"],
                         "solution_rel_diff": float(torch.linalg.norm(xm - x64) / torch.linalg.norm(x64))}
-    del x64, xm
+    del xm
+    # cphMG (continuous levels below the finest DG level): the reference's default multigrid for the
+    # sine application, in plain FP64 and mixed precision
+    xc64, rc64 = D.solve_unit_cube_sine(n, k, E.PREC_F64, E.PREC_F64, mg_type=E.MG_CPH)
+    xcm, rcm = D.solve_unit_cube_sine(n, k, E.PREC_F64E, E.PREC_F32, mg_type=E.MG_CPH)
+    out["cartesian_cphmg"] = {
+        "levels": rcm["levels"],
+        "plain_fp64": {kk: rc64[kk] for kk in ("iterations", "wall_seconds", "setup_seconds", "rn", "r0")},
+        "mixed": {kk: rcm[kk] for kk in ("iterations", "wall_seconds", "setup_seconds", "rn", "r0")},
+        "speedup_vs_plain_fp64_phmg": r64["wall_seconds"] / rcm["wall_seconds"],
+        "speedup_vs_mixed_phmg": rm["wall_seconds"] / rcm["wall_seconds"],
+        "solution_rel_diff": float(torch.linalg.norm(xcm - x64) / torch.linalg.norm(x64))}
+    del x64, xc64, xcm
     # configuration 3: curved 48^3, k = 5, mapping degree = k
     if not args.skip_curved:
         nc, kc = 48, 5
@@ -497,7 +509,8 @@ def run_component(args):
         op = E.LaplaceOperator(mesh, k, 1.0, E.PREC_F64E)
         if op.cartesian:
             op.tune()
-        mg = E.MultigridPreconditioner(op, mg_precision=E.PREC_F32)
+        mg = E.MultigridPreconditioner(op, mg_precision=E.PREC_F32,
+                                       mg_type=E.MG_CPH if args.mg_type == "cph" else E.MG_PH)
         r = torch.tensor(splitmix_uniform(op.n_dofs, 1), device="cuda")
         z = torch.empty_like(r)
         run = lambda: mg.vmult(z, r)
@@ -505,7 +518,8 @@ def run_component(args):
         for _ in range(2):
             mg.level_timings(r)
         level_ms = mg.level_timings(r)  # eager V-cycle with events per level (outside the timed region)
-        what = {"levels": [(l["n_cells"][0], l["degree"]) for l in info["levels"]], "mg_precision": "f32",
+        what = {"levels": [(l["n_cells"][0], l["degree"], "DG" if l["dg"] else "CG") for l in info["levels"]],
+                "mg_type": args.mg_type, "mg_precision": "f32",
                 "eager_level_ms": level_ms}
     for _ in range(max(args.warmup, 3)):
         run()
@@ -545,12 +559,16 @@ def run_learned(args):
     gen_s = time.perf_counter() - t0
     res = {}
     # plain_fp64: the reference's set-up on the GPU (FP64 operator, FP64 multigrid, BDF2 extrapolation)
-    runs = {"plain_fp64": ("extrapolation", E.PREC_F64, E.PREC_F64)}
+    # (the reference's TGV application uses cphMG: the *_cphmg runs)
+    runs = {"plain_fp64": ("extrapolation", E.PREC_F64, E.PREC_F64, E.MG_PH),
+            "plain_fp64_cphmg": ("extrapolation", E.PREC_F64, E.PREC_F64, E.MG_CPH)}
     for mode in ("extrapolation", "extrapolation3", "untrained", "learned"):
-        runs[mode] = (mode, E.PREC_F64E, E.PREC_F32)
-    for name, (mode, outer, mgp) in runs.items():
+        runs[mode] = (mode, E.PREC_F64E, E.PREC_F32, E.MG_PH)
+    for mode in ("extrapolation", "extrapolation3", "learned"):
+        runs[mode + "_cphmg"] = (mode, E.PREC_F64E, E.PREC_F32, E.MG_CPH)
+    for name, (mode, outer, mgp, mgt) in runs.items():
         seq = LG.PressureSequence(n_cells=32, degree=2, mode=mode, train_every=20, epochs=args.learned_epochs,
-                                  outer_precision=outer, mg_precision=mgp)
+                                  outer_precision=outer, mg_precision=mgp, mg_type=mgt)
         seq.diagnostics = args.learned_diagnostics
         for b in rhs:
             seq.step(b)
@@ -589,6 +607,10 @@ def run_learned(args):
             "iteration_gain_trained_vs_untrained": u["mean_iterations_second_half"] - l["mean_iterations_second_half"],
             "time_gain_second_half": e["mean_total_s_second_half"] / l["mean_total_s_second_half"],
             "speedup_mixed_learned_vs_plain_fp64": pf["mean_total_s_second_half"] / l["mean_total_s_second_half"],
+            "speedup_mixed_learned_cphmg_vs_plain_fp64_cphmg": res["plain_fp64_cphmg"]["mean_total_s_second_half"]
+            / res["learned_cphmg"]["mean_total_s_second_half"],
+            "iteration_gain_cphmg_learned_vs_extrapolation": res["extrapolation_cphmg"]["mean_iterations_second_half"]
+            - res["learned_cphmg"]["mean_iterations_second_half"],
             "iteration_gain_vs_third_order_ls": e3["mean_iterations_second_half"] - l["mean_iterations_second_half"],
             "time_gain_vs_third_order_ls": e3["mean_total_s_second_half"] / l["mean_total_s_second_half"],
             "results": res}
@@ -612,6 +634,7 @@ def main():
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--mode", default="apply", choices=["apply", "solve", "sweep", "learned", "operator", "vcycle"])
     ap.add_argument("--curved", action="store_true", help="operator / vcycle modes: deformed-cube mesh")
+    ap.add_argument("--mg-type", default="ph", choices=["ph", "cph"], help="vcycle mode: phMG or cphMG")
     ap.add_argument("--learned-steps", type=int, default=400)
     ap.add_argument("--learned-epochs", type=int, default=40)
     ap.add_argument("--learned-diagnostics", action="store_true")

@@ -1,26 +1,27 @@
 // Continuous levels of cphMG on Cartesian meshes (declarations and the algorithm in lattice.h).
 //
-// Apply: one CTA per TX x TY x TZ tile of output nodes.  The tile and a halo of k nodes per side
-// are read once into shared memory (constrained nodes and nodes outside a bounded lattice as
-// zero, periodic directions wrapped), then three 1D band passes run in shared memory:
+// Apply: one CTA per TX x TY x TZ tile of output nodes (extents and origins multiples of k, so
+// every row type is a compile-time constant and the unit-cell band coefficients are FMA operands
+// from the constant bank).  The tile and a halo of k nodes per side are read once into shared
+// memory (a warp per row, several rows in flight; nodes outside a bounded lattice read as zero,
+// periodic directions wrapped, constrained nodes zeroed afterwards), then three 1D band passes:
 //   z: a = M_z x, b = K_z x            (a thread per (x, y) column, the column in registers)
 //   y: c = M_y a, d = K_y a + M_y b    (a thread per (x, z) column; c, d reuse the input space)
-//   x: A x = K_x c + M_x d             (a thread per output node, coalesced store through the
-//                                       point epilogue; constrained nodes store src)
+//   x: A x = K_x c + M_x d             (a thread per row segment of k nodes)
+// and a coalesced store through the point epilogue (constrained nodes store src).
 // Global traffic is one read of src (plus the halo, mostly from L2) and one write of dst.
 #include <cuda_runtime.h>
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <set>
+#include <type_traits>
 
 #include "epilogue.cuh"
 #include "lattice.h"
 
 namespace exg {
-
-LatticeHost::~LatticeHost() {
-  if (coef_dev) cudaFree(coef_dev);
-}
 
 void make_lattice(const MeshInfo& m, int k, bool singular, LatticeHost& L) {
   EXG_CHECK(m.affine(), EXG_ERR_UNSUPPORTED, "continuous multigrid levels need a Cartesian mesh");
@@ -76,127 +77,298 @@ __device__ __forceinline__ bool dev_constrained(const LatticeMask& m, int gx, in
   return c;
 }
 
-template <int K>
-__device__ __forceinline__ int row_type(int g, int n, int periodic) {
-  if (!periodic) {
-    if (g == 0) return K;
-    if (g == n - 1) return K + 1;
-  }
-  return g % K;
-}
-
 // lattice coordinate of tile position g along a direction: wrapped when periodic, -1 outside
 __device__ __forceinline__ int lattice_coord(int g, int n, int periodic) {
   if (periodic) return ((g % n) + n) % n;
   return (g >= 0 && g < n) ? g : -1;
 }
 
-template <int K, class T>
-struct LatTile {
-  static constexpr int TX = 32;
-  // FP64 and high degrees: shorter register columns (no spills) and a tile that fits shared memory
-  static constexpr int TY = (K <= 4 && sizeof(T) == 4) ? 8 : 4;
-  static constexpr int TZ = (K <= 4 && sizeof(T) == 4) ? 8 : 4;
-  static constexpr int W = 2 * K + 1, NT = K + 2;
-  static constexpr int HX = TX + 2 * K, HY = TY + 2 * K, HZ = TZ + 2 * K;
-  static constexpr int NCOEF = 6 * NT * W;
-  static constexpr int SMEM = (NCOEF + HX * HY * HZ + 2 * HX * HY * TZ) * (int)sizeof(T);
+// Band tables of the unit cell for every degree, in constant memory: for degree K,
+// [mat (0 mass, 1 stiffness)][row type t = g mod K][o + K], o = -K..K, then the diagonal
+// corrections of a bounded line's first and last node [mat][2].  With tiles whose origin and
+// extent are multiples of K, every row type in the unrolled passes is a compile-time constant,
+// so each coefficient is an FMA operand from the constant bank.
+__host__ __device__ constexpr int band_size(int K) { return 2 * K * (2 * K + 1) + 4; }
+__host__ __device__ constexpr int band_off(int K) {
+  int s = 0;
+  for (int k = 1; k < K; ++k) s += band_size(k);
+  return s;
+}
+constexpr int BAND_TOTAL = band_off(LAT_KMAX + 1);
+__constant__ float c_band_f[BAND_TOTAL];
+__constant__ double c_band_d[BAND_TOTAL];
+
+template <class T>
+__device__ __forceinline__ T band(int i);
+template <>
+__device__ __forceinline__ float band<float>(int i) {
+  return c_band_f[i];
+}
+template <>
+__device__ __forceinline__ double band<double>(int i) {
+  return c_band_d[i];
+}
+
+// unit-cell band table of degree K (row types 0..K-1; a bounded line's end nodes are type 0 rows
+// whose outside neighbours are zero, minus the other cell's diagonal entry)
+static void unit_band(int K, std::vector<double>& out) {
+  FE1D fe;
+  fe.init(K, K + 1);
+  const int n = K + 1, W = 2 * K + 1;
+  out.assign(band_size(K), 0.0);
+  for (int mat = 0; mat < 2; ++mat) {
+    const std::vector<double>& E = mat == 0 ? fe.M : fe.K;
+    double* c = &out[mat * K * W];
+    for (int t = 1; t < K; ++t)
+      for (int j = 0; j <= K; ++j) c[t * W + (j - t) + K] += E[t * n + j];
+    for (int j = 0; j <= K; ++j) {
+      c[(j - K) + K] += E[K * n + j];
+      c[j + K] += E[0 * n + j];
+    }
+    out[2 * K * W + mat * 2 + 0] = E[K * n + K];  // first node: no left cell
+    out[2 * K * W + mat * 2 + 1] = E[0 * n + 0];  // last node: no right cell
+  }
+}
+
+void lattice_prepare(LatticeHost& L, int precision) {
+  (void)L;
+  (void)precision;
+  static std::mutex mu;
+  static std::set<int> done;
+  int dev = 0;
+  EXG_CUDA(cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lock(mu);
+  if (done.count(dev)) return;
+  std::vector<double> all(BAND_TOTAL, 0.0), one;
+  for (int K = 1; K <= LAT_KMAX; ++K) {
+    unit_band(K, one);
+    std::copy(one.begin(), one.end(), all.begin() + band_off(K));
+  }
+  std::vector<float> allf(all.begin(), all.end());
+  EXG_CUDA(cudaMemcpyToSymbol(c_band_d, all.data(), all.size() * sizeof(double)));
+  EXG_CUDA(cudaMemcpyToSymbol(c_band_f, allf.data(), allf.size() * sizeof(float)));
+  done.insert(dev);
+}
+
+template <class T>
+struct LatParams {
+  LatticeMask m;
+  T hm[3], hk[3];  // mass scale h_d and stiffness scale 1 / h_d
 };
 
+// the largest multiple of K not above `want` (at least K)
+__host__ __device__ constexpr int tile_mult(int K, int want) { return K * (want / K > 0 ? want / K : 1); }
+
 template <int K, class T>
-__global__ void __launch_bounds__(256) lattice_apply_kernel(const __grid_constant__ LatticeMask m,
-                                                            const T* __restrict__ coef_g,
+struct LatTile {
+  static constexpr bool F32 = sizeof(T) == 4;
+  static constexpr int TX = F32 ? tile_mult(K, 32) : (K <= 4 ? tile_mult(K, 16) : tile_mult(K, 8));
+  static constexpr int TY = F32 ? tile_mult(K, 8) : tile_mult(K, 4);
+  static constexpr int TZ = TY;
+  static constexpr int W = 2 * K + 1;
+  static constexpr int HX = TX + 2 * K, HY = TY + 2 * K, HZ = TZ + 2 * K;
+  static constexpr int HXP = HX | 1;  // odd row stride of c, d (conflict-free x pass)
+  static constexpr int TXP = TX | 1;  // odd row stride of the x pass results
+  // the input tile, later c and d (which need more room than the tile only for K = 1)
+  static constexpr int IN_WORDS = HX * HY * HZ > 2 * HXP * TY * TZ ? HX * HY * HZ : 2 * HXP * TY * TZ;
+  static constexpr int SMEM = (IN_WORDS + 2 * HX * HY * TZ) * (int)sizeof(T);
+  static_assert(TXP * TY * TZ <= HX * HY * TZ, "results must fit a");
+};
+
+// compile-time loop: f(std::integral_constant<int, I>) for I = B..E-1
+template <int B, int E, class F>
+__device__ __forceinline__ void static_for(F&& f) {
+  if constexpr (B < E) {
+    f(std::integral_constant<int, B>{});
+    static_for<B + 1, E>(f);
+  }
+}
+
+// row g of a 1D band pass on the column v (v[T0 + o + K] = x_{g+o}), row type T0 mod K: mass and
+// stiffness sums of the unit cell (every coefficient index a constant, so the coefficient is an
+// FMA operand from the constant bank), with the diagonal correction of a bounded line's end nodes
+template <int K, int T0, bool WANT_K, class T>
+__device__ __forceinline__ void band_row(const T* v, int g, int n, int periodic, T& sm, T& sk) {
+  constexpr int W = 2 * K + 1, B = band_off(K), t = T0 % K;
+  sm = T(0);
+  sk = T(0);
+  static_for<0, W>([&](auto oc) {
+    constexpr int o = decltype(oc)::value;
+    if constexpr (t == 0 || (o >= K - t && o <= 2 * K - t)) {
+      sm += band<T>(B + (0 * K + t) * W + o) * v[T0 + o];
+      if constexpr (WANT_K) sk += band<T>(B + (1 * K + t) * W + o) * v[T0 + o];
+    }
+  });
+  if constexpr (t == 0) {
+    if (!periodic && (g == 0 || g == n - 1)) {
+      const bool first = g == 0;
+      sm -= (first ? band<T>(B + 2 * K * W + 0) : band<T>(B + 2 * K * W + 1)) * v[T0 + K];
+      if constexpr (WANT_K) sk -= (first ? band<T>(B + 2 * K * W + 2) : band<T>(B + 2 * K * W + 3)) * v[T0 + K];
+    }
+  }
+}
+
+template <int K, class T>
+__global__ void __launch_bounds__(256) lattice_apply_kernel(const __grid_constant__ LatParams<T> P,
                                                             const T* __restrict__ src, T* __restrict__ dst,
                                                             const __grid_constant__ PointEpilogue ep) {
   using G = LatTile<K, T>;
-  constexpr int TX = G::TX, TY = G::TY, TZ = G::TZ, W = G::W, NT = G::NT, HX = G::HX, HY = G::HY, HZ = G::HZ;
+  constexpr int TX = G::TX, TY = G::TY, TZ = G::TZ, HX = G::HX, HY = G::HY, HZ = G::HZ, HXP = G::HXP,
+                TXP = G::TXP, NTH = 256;
+  const LatticeMask& m = P.m;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* coef = reinterpret_cast<T*>(smem_raw);  // [dir][mat][type][W]
-  T* in = coef + G::NCOEF;                   // HX*HY*HZ input tile; later c, d
-  T* a = in + HX * HY * HZ;                  // HX*HY*TZ
+  T* in = reinterpret_cast<T*>(smem_raw);  // HX*HY*HZ input tile; later c, d
+  T* a = in + G::IN_WORDS;                 // HX*HY*TZ; later the x pass results
   T* b = a + HX * HY * TZ;
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  for (int i = tid; i < G::NCOEF; i += nt) coef[i] = coef_g[i];
-  for (int i = tid; i < HX * HY * HZ; i += nt) {
-    const int lx = i % HX, ly = (i / HX) % HY, lz = i / (HX * HY);
-    const int gx = lattice_coord(x0 + lx - K, m.n[0], m.periodic[0]);
-    const int gy = lattice_coord(y0 + ly - K, m.n[1], m.periodic[1]);
-    const int gz = lattice_coord(z0 + lz - K, m.n[2], m.periodic[2]);
-    T v = T(0);
-    if (gx >= 0 && gy >= 0 && gz >= 0 && !dev_constrained(m, gx, gy, gz))
-      v = src[gx + (long long)m.n[0] * (gy + (long long)m.n[1] * gz)];
-    in[i] = v;
+  const int tid = threadIdx.x;
+  // tile load: a warp per row of HX nodes, U rows in flight per warp; a lane's (at most two) x
+  // positions are found once.  Constrained nodes are zeroed afterwards, in the tiles that hold any.
+  const int lane = tid & 31, warp = tid >> 5;
+  static_assert(HX <= 64, "two x positions per lane");
+  constexpr int U = sizeof(T) == 4 ? 8 : 4, ROWS_IN = HY * HZ;
+  int gxs[2];
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    const int lx = lane + 32 * c;
+    gxs[c] = lx < HX ? lattice_coord(x0 + lx - K, m.n[0], m.periodic[0]) : -1;
+  }
+  for (int r0 = warp * U; r0 < ROWS_IN; r0 += (NTH / 32) * U) {
+    T vals[U][2];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int r = r0 + u;
+      const int ly = r % HY, lz = r / HY;
+      const int gy = lattice_coord(y0 + ly - K, m.n[1], m.periodic[1]);
+      const int gz = lattice_coord(z0 + lz - K, m.n[2], m.periodic[2]);
+      const bool rok = r < ROWS_IN && gy >= 0 && gz >= 0;
+      const int rbase = m.n[0] * (gy + m.n[1] * gz);
+#pragma unroll
+      for (int c = 0; c < 2; ++c) vals[u][c] = (rok && gxs[c] >= 0) ? src[rbase + gxs[c]] : T(0);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u)
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int lx = lane + 32 * c;
+        if (r0 + u < ROWS_IN && lx < HX) in[(r0 + u) * HX + lx] = vals[u][c];
+      }
   }
   __syncthreads();
-  // z pass
   {
-    const T* Mz = coef + (2 * 2 + 0) * NT * W;
-    const T* Kz = coef + (2 * 2 + 1) * NT * W;
-    for (int col = tid; col < HX * HY; col += nt) {
-      T v[HZ];
+    // Dirichlet planes inside the tile (tile position of lattice plane 0 and n-1 per direction)
+    int plane[6];
+    bool any = false;
 #pragma unroll
-      for (int z = 0; z < HZ; ++z) v[z] = in[z * HX * HY + col];
+    for (int f = 0; f < 6; ++f) {
+      const int dir = f / 2, o0 = dir == 0 ? x0 : (dir == 1 ? y0 : z0), H = dir == 0 ? HX : (dir == 1 ? HY : HZ);
+      const int lp = (f % 2 == 0 ? 0 : m.n[dir] - 1) - o0 + K;
+      plane[f] = (!m.periodic[dir] && m.dirichlet[f] && lp >= 0 && lp < H) ? lp : -1;
+      any |= plane[f] >= 0;
+    }
+    if (any) {
 #pragma unroll
-      for (int tz = 0; tz < TZ; ++tz) {
-        const int ty = row_type<K>(min(z0 + tz, m.n[2] - 1), m.n[2], m.periodic[2]);
-        T sa = T(0), sb = T(0);
-#pragma unroll
-        for (int o = 0; o < W; ++o) {
-          sa += Mz[ty * W + o] * v[tz + o];
-          sb += Kz[ty * W + o] * v[tz + o];
+      for (int f = 0; f < 6; ++f) {
+        if (plane[f] < 0) continue;
+        const int dir = f / 2;
+        const int na = dir == 0 ? HY : HX, nb = dir == 2 ? HY : HZ;  // the plane's other two extents
+        for (int i = tid; i < na * nb; i += NTH) {
+          const int ia = i % na, ib = i / na;
+          const int lx = dir == 0 ? plane[f] : ia, ly = dir == 1 ? plane[f] : (dir == 0 ? ia : ib),
+                    lz = dir == 2 ? plane[f] : ib;
+          in[(lz * HY + ly) * HX + lx] = T(0);
         }
-        a[tz * HX * HY + col] = sa;
-        b[tz * HX * HY + col] = sb;
       }
     }
+    if (m.pin_first && tid == 0) {  // node 0 of a singular operator (wherever periodic copies sit)
+      for (int lz = 0; lz < HZ; ++lz)
+        if (lattice_coord(z0 + lz - K, m.n[2], m.periodic[2]) == 0)
+          for (int ly = 0; ly < HY; ++ly)
+            if (lattice_coord(y0 + ly - K, m.n[1], m.periodic[1]) == 0)
+              for (int lx = 0; lx < HX; ++lx)
+                if (lattice_coord(x0 + lx - K, m.n[0], m.periodic[0]) == 0) in[(lz * HY + ly) * HX + lx] = T(0);
+    }
+    if (any || m.pin_first) __syncthreads();
+  }
+  // z pass: a = M_z x, b = K_z x on the haloed (x, y) plane
+  for (int col = tid; col < HX * HY; col += NTH) {
+    T v[HZ];
+#pragma unroll
+    for (int z = 0; z < HZ; ++z) v[z] = in[z * HX * HY + col];
+    static_for<0, TZ>([&](auto tc) {
+      constexpr int tz = decltype(tc)::value;
+      T sm, sk;
+      band_row<K, tz, true, T>(v, z0 + tz, m.n[2], m.periodic[2], sm, sk);
+      a[tz * HX * HY + col] = sm * P.hm[2];
+      b[tz * HX * HY + col] = sk * P.hk[2];
+    });
   }
   __syncthreads();
-  // y pass: columns (x, z) of the haloed x range; c, d overwrite the input tile
+  // y pass: c = M_y a, d = K_y a + M_y b on the haloed x range (c, d overwrite the input tile)
   T* c = in;
-  T* d = in + HX * TY * TZ;
-  {
-    const T* My = coef + (1 * 2 + 0) * NT * W;
-    const T* Ky = coef + (1 * 2 + 1) * NT * W;
-    for (int col = tid; col < HX * TZ; col += nt) {
-      const int lx = col % HX, tz = col / HX;
-      T va[HY], vb[HY];
+  T* d = in + HXP * TY * TZ;
+  for (int col = tid; col < HX * TZ; col += NTH) {
+    const int lx = col % HX, tz = col / HX;
+    T va[HY], vb[HY];
 #pragma unroll
-      for (int y = 0; y < HY; ++y) {
-        va[y] = a[(tz * HY + y) * HX + lx];
-        vb[y] = b[(tz * HY + y) * HX + lx];
-      }
-#pragma unroll
-      for (int ty = 0; ty < TY; ++ty) {
-        const int tp = row_type<K>(min(y0 + ty, m.n[1] - 1), m.n[1], m.periodic[1]);
-        T sc = T(0), sd = T(0);
-#pragma unroll
-        for (int o = 0; o < W; ++o) {
-          sc += My[tp * W + o] * va[ty + o];
-          sd += Ky[tp * W + o] * va[ty + o] + My[tp * W + o] * vb[ty + o];
-        }
-        c[(tz * TY + ty) * HX + lx] = sc;
-        d[(tz * TY + ty) * HX + lx] = sd;
-      }
+    for (int y = 0; y < HY; ++y) {
+      va[y] = a[(tz * HY + y) * HX + lx];
+      vb[y] = b[(tz * HY + y) * HX + lx];
     }
+    static_for<0, TY>([&](auto tc) {
+      constexpr int ty = decltype(tc)::value;
+      T ma, ka, mb, kb;
+      band_row<K, ty, true, T>(va, y0 + ty, m.n[1], m.periodic[1], ma, ka);
+      band_row<K, ty, false, T>(vb, y0 + ty, m.n[1], m.periodic[1], mb, kb);
+      c[(tz * TY + ty) * HXP + lx] = ma * P.hm[1];
+      d[(tz * TY + ty) * HXP + lx] = ka * P.hk[1] + mb * P.hm[1];
+    });
   }
   __syncthreads();
-  // x pass and store
-  const T* Mx = coef + (0 * 2 + 0) * NT * W;
-  const T* Kx = coef + (0 * 2 + 1) * NT * W;
-  for (int i = tid; i < TX * TY * TZ; i += nt) {
-    const int tx = i % TX, ty = (i / TX) % TY, tz = i / (TX * TY);
-    const int gx = x0 + tx, gy = y0 + ty, gz = z0 + tz;
-    if (gx >= m.n[0] || gy >= m.n[1] || gz >= m.n[2]) continue;
-    const int tp = row_type<K>(gx, m.n[0], m.periodic[0]);
-    const T* cr = c + (tz * TY + ty) * HX + tx;
-    const T* dr = d + (tz * TY + ty) * HX + tx;
-    T s = T(0);
+  // x pass: a thread per (row, cell segment of K nodes), rows across the lanes
+  T* res = a;
+  constexpr int SEG = TX / K, ROWS = TY * TZ;
+  for (int it = tid; it < SEG * ROWS; it += NTH) {
+    const int row = it % ROWS, q = it / ROWS;
+    const T* cr = c + row * HXP + q * K;
+    const T* dr = d + row * HXP + q * K;
+    T vc[3 * K], vd[3 * K];
 #pragma unroll
-    for (int o = 0; o < W; ++o) s += Kx[tp * W + o] * cr[o] + Mx[tp * W + o] * dr[o];
-    const long long gi = gx + (long long)m.n[0] * (gy + (long long)m.n[1] * gz);
-    if (dev_constrained(m, gx, gy, gz)) s = src[gi];
-    epilogue_store<T>(ep, dst, gi, src, s);
+    for (int j = 0; j < 3 * K; ++j) {
+      vc[j] = cr[j];
+      vd[j] = dr[j];
+    }
+    const int gq = x0 + q * K;
+    static_for<0, K>([&](auto lc) {
+      constexpr int l = decltype(lc)::value;
+      T mc, kc, md, kd;
+      band_row<K, l, true, T>(vc, gq + l, m.n[0], m.periodic[0], mc, kc);
+      band_row<K, l, false, T>(vd, gq + l, m.n[0], m.periodic[0], md, kd);
+      res[row * TXP + q * K + l] = kc * P.hk[0] + md * P.hm[0];
+    });
+  }
+  __syncthreads();
+  // coalesced store through the point epilogue, a warp per output row (U rows in flight);
+  // constrained nodes keep src
+  static_assert(TX <= 32, "one x position per lane");
+  const int gx = x0 + lane;
+  const bool xin = lane < TX && gx < m.n[0];
+  const bool xc = !m.periodic[0] && ((gx == 0 && m.dirichlet[0]) || (gx == m.n[0] - 1 && m.dirichlet[1]));
+  constexpr int ROWS_OUT = TY * TZ;
+  for (int r0 = warp * U; r0 < ROWS_OUT; r0 += (NTH / 32) * U) {
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int row = r0 + u;
+      const int ty = row % TY, tz = row / TY;
+      const int gy = y0 + ty, gz = z0 + tz;
+      if (row >= ROWS_OUT || !xin || gy >= m.n[1] || gz >= m.n[2]) continue;
+      const bool rc = (!m.periodic[1] && ((gy == 0 && m.dirichlet[2]) || (gy == m.n[1] - 1 && m.dirichlet[3]))) ||
+                      (!m.periodic[2] && ((gz == 0 && m.dirichlet[4]) || (gz == m.n[2] - 1 && m.dirichlet[5])));
+      const int gi = gx + m.n[0] * (gy + m.n[1] * gz);
+      T v = res[row * TXP + lane];
+      if (xc || rc || (m.pin_first && gx == 0 && gy == 0 && gz == 0)) v = src[gi];
+      epilogue_store<T>(ep, dst, gi, src, v);
+    }
   }
 }
 
@@ -208,25 +380,21 @@ static void launch_apply(const LatticeHost& L, const T* src, T* dst, const Point
   dim3 grid((L.mask.n[0] + G::TX - 1) / G::TX, (L.mask.n[1] + G::TY - 1) / G::TY,
             (L.mask.n[2] + G::TZ - 1) / G::TZ);
   EXG_CHECK(grid.y <= 65535 && grid.z <= 65535, EXG_ERR_UNSUPPORTED, "lattice too long in y or z");
-  kern<<<grid, 256, G::SMEM, s>>>(L.mask, (const T*)L.coef_dev, src, dst, ep);
+  LatParams<T> P;
+  P.m = L.mask;
+  for (int e = 0; e < 3; ++e) {
+    P.hm[e] = (T)L.h[e];
+    P.hk[e] = (T)(1.0 / L.h[e]);
+  }
+  kern<<<grid, 256, G::SMEM, s>>>(P, src, dst, ep);
   EXG_CUDA(cudaGetLastError());
-}
-
-template <class T>
-static void ensure_coef(LatticeHost& L, int prec) {
-  if (L.coef_dev && L.coef_prec == prec) return;
-  if (L.coef_dev) cudaFree(L.coef_dev);
-  std::vector<T> c(L.coef.begin(), L.coef.end());
-  EXG_CUDA(cudaMalloc(&L.coef_dev, c.size() * sizeof(T)));
-  EXG_CUDA(cudaMemcpy(L.coef_dev, c.data(), c.size() * sizeof(T), cudaMemcpyHostToDevice));
-  L.coef_prec = prec;
 }
 
 template <class T>
 static void apply_t(LatticeHost& L, const T* src, T* dst, const PointEpilogue& ep, cudaStream_t s) {
   switch (L.k) {
-#define EXG_LAT_CASE(KK) \
-  case KK:               \
+#define EXG_LAT_CASE(KK)                     \
+  case KK:                                   \
     launch_apply<KK, T>(L, src, dst, ep, s); \
     break;
     EXG_LAT_CASE(1)
@@ -243,21 +411,12 @@ static void apply_t(LatticeHost& L, const T* src, T* dst, const PointEpilogue& e
   }
 }
 
-void lattice_prepare(LatticeHost& L, int precision) {
-  if (precision == EXG_PREC_F32)
-    ensure_coef<float>(L, precision);
-  else
-    ensure_coef<double>(L, precision);
-}
-
 void lattice_apply(LatticeHost& L, int precision, const void* src, void* dst, cudaStream_t s,
                    const PointEpilogue& ep) {
   if (precision == EXG_PREC_F32) {
-    ensure_coef<float>(L, precision);
     apply_t<float>(L, (const float*)src, (float*)dst, ep, s);
   } else {
     EXG_CHECK(precision == EXG_PREC_F64, EXG_ERR_UNSUPPORTED, "continuous levels compute in FP32 or FP64");
-    ensure_coef<double>(L, precision);
     apply_t<double>(L, (const double*)src, (double*)dst, ep, s);
   }
 }
@@ -329,40 +488,54 @@ void lattice_diagonal(LatticeHost& L, int precision, void* diag, bool invert, cu
 // restriction is the transpose, dropping contributions to constrained coarse nodes)
 // ------------------------------------------------------------------------------------------
 
-// one 1D pass along dir: out(.., r, ..) = sum_t val[r][t] in(.., col[r][t], ..); the first pass
-// reads constrained input nodes as zero (mask_in), the last one adds into out at its
-// unconstrained nodes (accumulate)
-template <class T>
+// one 1D pass along dir: out(.., r, ..) = sum_t val[r][t] in(.., col[r][t], ..) with W taps per
+// row (rows padded with zero taps; W a compile-time constant so that all loads of a row are in
+// flight together); the first pass reads constrained input nodes as zero (mask_in), the last one
+// adds into out at its unconstrained nodes (accumulate).  Extents are below 2^31.
+template <class T, int W>
 __global__ void lattice_pass_kernel(const T* __restrict__ in, T* __restrict__ out, int o0, int o1, int o2, int dir,
-                                    int n_in_dir, const int* __restrict__ col, const T* __restrict__ val, int w,
+                                    int n_in_dir, const int* __restrict__ col, const T* __restrict__ val,
                                     const __grid_constant__ LatticeMask min, int mask_in,
                                     const __grid_constant__ LatticeMask mout, int accumulate) {
-  const long long total = (long long)o0 * o1 * o2;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
-       i += (long long)gridDim.x * blockDim.x) {
-    int c[3] = {(int)(i % o0), (int)((i / o0) % o1), (int)(i / ((long long)o0 * o1))};
-    const int r = dir == 0 ? c[0] : (dir == 1 ? c[1] : c[2]);
-    int di[3] = {o0, o1, o2};
-    di[dir] = n_in_dir;
-    const long long stride = dir == 0 ? 1 : (dir == 1 ? (long long)di[0] : (long long)di[0] * di[1]);
-    int ci[3] = {c[0], c[1], c[2]};
-    ci[dir] = 0;
-    const long long base = ci[0] + (long long)di[0] * (ci[1] + (long long)di[1] * ci[2]);
+  const int total = o0 * o1 * o2;
+  const int i0 = dir == 0 ? n_in_dir : o0;  // input extents
+  const int i1 = dir == 1 ? n_in_dir : o1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int cx = i % o0, rest = i / o0, cy = rest % o1, cz = rest / o1;
+    const int r = dir == 0 ? cx : (dir == 1 ? cy : cz);
+    const int stride = dir == 0 ? 1 : (dir == 1 ? i0 : i0 * i1);
+    const int base = (dir == 0 ? 0 : cx) + i0 * ((dir == 1 ? 0 : cy) + i1 * (dir == 2 ? 0 : cz));
+    int cs[W];
+    T vs[W], xs[W];
+#pragma unroll
+    for (int t = 0; t < W; ++t) {
+      cs[t] = col[r * W + t];
+      vs[t] = val[r * W + t];
+    }
+#pragma unroll
+    for (int t = 0; t < W; ++t) xs[t] = in[base + cs[t] * stride];
     T acc = T(0);
-    for (int t = 0; t < w; ++t) {
-      const int j = col[r * w + t];
-      if (mask_in) {
-        ci[dir] = j;
-        if (dev_constrained(min, ci[0], ci[1], ci[2])) continue;
-      }
-      acc += val[r * w + t] * in[base + j * stride];
+#pragma unroll
+    for (int t = 0; t < W; ++t) {
+      bool zero = false;
+      if (mask_in)
+        zero = dev_constrained(min, dir == 0 ? cs[t] : cx, dir == 1 ? cs[t] : cy, dir == 2 ? cs[t] : cz);
+      acc += zero ? T(0) : vs[t] * xs[t];
     }
     if (accumulate) {
-      if (!dev_constrained(mout, c[0], c[1], c[2])) out[i] += acc;
+      if (!dev_constrained(mout, cx, cy, cz)) out[i] += acc;
     } else {
       out[i] = acc;
     }
   }
+}
+
+// tap counts with a compiled pass
+static int padded_width(int w) {
+  for (int c : {2, 3, 4, 5, 6, 8, 10, 12, 17})
+    if (w <= c) return c;
+  EXG_CHECK(false, EXG_ERR_UNSUPPORTED, "transfer row too wide");
+  return 0;
 }
 
 // c-transfer: every DG DoF reads its lattice node
@@ -462,8 +635,9 @@ void LatticeTransfer::setup(const LatticeHost& coarse, const LatticeHost& fine, 
     const int Ncd = coarse.N[d], Nfd = fine.N[d], nf = mf.n[d], nc = mc.n[d];
     const bool per = mc.periodic[d] != 0, is_h = Nfd != Ncd;
     EXG_CHECK(Nfd == Ncd || Nfd == 2 * Ncd, EXG_ERR_UNSUPPORTED, "unsupported continuous transfer");
-    // prolongation rows: fine node -> kc+1 coarse nodes of the coarse cell around it
-    const int w = kc + 1;
+    // prolongation rows: fine node -> kc+1 coarse nodes of the coarse cell around it (zero taps pad
+    // the row to a compiled width)
+    const int w = padded_width(kc + 1);
     std::vector<int> pc((size_t)nf * w, 0);
     std::vector<double> pv((size_t)nf * w, 0.0);
     std::vector<char> done(nf, 0);
@@ -485,9 +659,10 @@ void LatticeTransfer::setup(const LatticeHost& coarse, const LatticeHost& fine, 
     // restriction rows: the transpose, padded to the widest coarse row
     std::vector<std::vector<std::pair<int, double>>> rows(nc);
     for (int g = 0; g < nf; ++g)
-      for (int j = 0; j < w; ++j) rows[pc[(size_t)g * w + j]].push_back({g, pv[(size_t)g * w + j]});
+      for (int j = 0; j <= kc; ++j) rows[pc[(size_t)g * w + j]].push_back({g, pv[(size_t)g * w + j]});
     int wr_d = 1;
     for (auto& r : rows) wr_d = std::max(wr_d, (int)r.size());
+    wr_d = padded_width(wr_d);
     std::vector<int> rc((size_t)nc * wr_d, 0);
     std::vector<double> rv((size_t)nc * wr_d, 0.0);
     for (int j = 0; j < nc; ++j)
@@ -526,10 +701,29 @@ static void pass(const LatticeTransfer& t, const T* in, T* out, const int dims_o
                  const int* col, const void* val, int w, const LatticeMask* min, const LatticeMask* mout,
                  cudaStream_t s) {
   const long long total = (long long)dims_out[0] * dims_out[1] * dims_out[2];
+  EXG_CHECK(total < (1LL << 31), EXG_ERR_INVALID, "lattice too large");
   LatticeMask none{};
-  lattice_pass_kernel<T><<<grid_for(total), 256, 0, s>>>(in, out, dims_out[0], dims_out[1], dims_out[2], dir, n_in_dir,
-                                                         col, (const T*)val, w, min ? *min : none, min ? 1 : 0,
-                                                         mout ? *mout : none, mout ? 1 : 0);
+  const int g = grid_for(total);
+#define EXG_PASS(WW)                                                                                          \
+  case WW:                                                                                                    \
+    lattice_pass_kernel<T, WW><<<g, 256, 0, s>>>(in, out, dims_out[0], dims_out[1], dims_out[2], dir, n_in_dir, \
+                                                 col, (const T*)val, min ? *min : none, min ? 1 : 0,          \
+                                                 mout ? *mout : none, mout ? 1 : 0);                          \
+    break;
+  switch (w) {
+    EXG_PASS(2)
+    EXG_PASS(3)
+    EXG_PASS(4)
+    EXG_PASS(5)
+    EXG_PASS(6)
+    EXG_PASS(8)
+    EXG_PASS(10)
+    EXG_PASS(12)
+    EXG_PASS(17)
+    default:
+      EXG_CHECK(false, EXG_ERR_UNSUPPORTED, "transfer row width");
+  }
+#undef EXG_PASS
   EXG_CUDA(cudaGetLastError());
   (void)t;
 }

@@ -38,10 +38,7 @@ struct LatticeHost {
   double h[3];
   // band coefficients [dir][0 = mass, 1 = stiffness][row type 0..k+1][o + k], o = -k..k
   std::vector<double> coef;
-  void* coef_dev = nullptr;  // the table in the operator's storage precision
-  int coef_prec = -1;
   long long size() const { return (long long)mask.n[0] * mask.n[1] * mask.n[2]; }
-  ~LatticeHost();
 };
 
 // lattice of the mesh m at degree k (singular: pin node 0)
@@ -52,7 +49,8 @@ bool lattice_constrained(const LatticeMask& m, int gx, int gy, int gz);
 void lattice_apply(LatticeHost& L, int precision, const void* src, void* dst, cudaStream_t s,
                    const PointEpilogue& ep = PointEpilogue());
 void lattice_diagonal(LatticeHost& L, int precision, void* diag, bool invert, cudaStream_t s);
-// uploads the band table in `precision` (synchronous: call before any stream capture)
+// uploads the unit-cell band tables to the current device once (synchronous: call before any
+// stream capture)
 void lattice_prepare(LatticeHost& L, int precision);
 
 // transfer between level l-1 (continuous) and level l (continuous, or the discontinuous level of

@@ -66,7 +66,7 @@ class PoissonProblem:
     poisson/spatial_discretization/operator.cpp:261-473)."""
 
     def __init__(self, mesh_kwargs, degree, outer_precision=E.PREC_F64, mg_precision=E.PREC_F32,
-                 use_graph=True, coarse_double=False, singular=False, tune=True, ip_factor=1.0):
+                 use_graph=True, coarse_double=False, singular=False, tune=True, ip_factor=1.0, mg_type=E.MG_PH):
         t0 = time.perf_counter()
         self.mesh = E.Mesh(**mesh_kwargs)
         self.op = E.LaplaceOperator(self.mesh, degree, ip_factor, outer_precision)
@@ -74,7 +74,7 @@ class PoissonProblem:
         if tune and self.op.cartesian:
             self.op.tune()
         self.mg = E.MultigridPreconditioner(self.op, mg_precision=mg_precision, use_graph=use_graph,
-                                            coarse_double=coarse_double, singular=singular)
+                                            coarse_double=coarse_double, singular=singular, mg_type=mg_type)
         self.setup_seconds = time.perf_counter() - t0
         self.degree = degree
         self.mesh_kwargs = mesh_kwargs
@@ -113,19 +113,20 @@ def deformed_unit_cube(n, amp=0.08, freq=2, mapping_degree=None, degree=5):
                 mapping_degree=mapping_degree or degree)
 
 
-def solve_unit_cube_sine(n, degree, outer_precision, mg_precision, curved=False, use_graph=True, rel_tol=1e-10):
+def solve_unit_cube_sine(n, degree, outer_precision, mg_precision, curved=False, use_graph=True, rel_tol=1e-10,
+                         mg_type=E.MG_PH):
     """-Laplace u = f on [0,1]^3, u = prod sin(pi x_d) (Dirichlet data = u), returns timings."""
     import torch
 
     kw = deformed_unit_cube(n, degree=degree) if curved else unit_cube(n)
-    prob = PoissonProblem(kw, degree, outer_precision, mg_precision, use_graph=use_graph)
+    prob = PoissonProblem(kw, degree, outer_precision, mg_precision, use_graph=use_graph, mg_type=mg_type)
     u, f, _ = sine_functions(math.pi)
     b = assemble_rhs(prob.rhs_operator(), f=f, g=u)
     x, r = prob.solve(b, rel_tol=rel_tol)
     r["setup_seconds"] = prob.setup_seconds
     r["n_dofs"] = prob.op.n_dofs
     info = prob.mg.info()
-    r["levels"] = [(l["n_cells"][0], l["degree"]) for l in info["levels"]]
+    r["levels"] = [(l["n_cells"][0], l["degree"], "DG" if l["dg"] else "CG") for l in info["levels"]]
     r["coarse_iterations"] = info["coarse_iterations"]
     del prob
     torch.cuda.synchronize()

@@ -57,7 +57,7 @@ def _rms(t):
 class PressureSequence:
     def __init__(self, n_cells=32, degree=2, length=6.283185307179586, mode="learned", train_every=20,
                  epochs=40, lr=1e-4, buffer=20, hidden=32, seed=1, tol=1e-10, outer_precision=E.PREC_F64E,
-                 mg_precision=E.PREC_F32):
+                 mg_precision=E.PREC_F32, mg_type=E.MG_PH):
         import torch
 
         self.torch = torch
@@ -65,7 +65,7 @@ class PressureSequence:
         self.mesh = E.Mesh(**kw)
         self.op = E.LaplaceOperator(self.mesh, degree, 1.0, outer_precision)
         self.op.tune()
-        self.mg = E.MultigridPreconditioner(self.op, mg_precision=mg_precision, singular=True)
+        self.mg = E.MultigridPreconditioner(self.op, mg_precision=mg_precision, singular=True, mg_type=mg_type)
         self.n_cells = n_cells
         self.nc = n_cells ** 3
         self.dpc = (degree + 1) ** 3

@@ -5,8 +5,9 @@
 // from the constant bank).  The tile and a halo of k nodes per side are read once into shared
 // memory (a warp per row, several rows in flight; nodes outside a bounded lattice read as zero,
 // periodic directions wrapped, constrained nodes zeroed afterwards), then three 1D band passes:
-//   z: a = M_z x, b = K_z x            (a thread per (x, y) column, the column in registers)
-//   y: c = M_y a, d = K_y a + M_y b    (a thread per (x, z) column; c, d reuse the input space)
+//   z: a = M_z x, b = K_z x            (a thread per (x, y) column, the column in registers;
+//                                       a, b written over the tile where they fit)
+//   y: c = M_y a, d = K_y a + M_y b    (a thread per (x, z) column)
 //   x: A x = K_x c + M_x d             (a thread per row segment of k nodes)
 // and a coalesced store through the point epilogue (constrained nodes store src).
 // Global traffic is one read of src (plus the halo, mostly from L2) and one write of dst.
@@ -159,9 +160,10 @@ struct LatParams {
 // the largest multiple of K not above `want` (at least K)
 __host__ __device__ constexpr int tile_mult(int K, int want) { return K * (want / K > 0 ? want / K : 1); }
 
-template <int K, class T>
+// SMALL: quarter-size tiles for lattices too small to fill the GPU with full ones
+template <int K, class T, bool SMALL>
 struct LatTile {
-  static constexpr bool F32 = sizeof(T) == 4;
+  static constexpr bool F32 = sizeof(T) == 4 && !SMALL;
   static constexpr int TX = F32 ? tile_mult(K, 32) : (K <= 4 ? tile_mult(K, 16) : tile_mult(K, 8));
   static constexpr int TY = F32 ? tile_mult(K, 8) : tile_mult(K, 4);
   static constexpr int TZ = TY;
@@ -169,10 +171,21 @@ struct LatTile {
   static constexpr int HX = TX + 2 * K, HY = TY + 2 * K, HZ = TZ + 2 * K;
   static constexpr int HXP = HX | 1;  // odd row stride of c, d (conflict-free x pass)
   static constexpr int TXP = TX | 1;  // odd row stride of the x pass results
-  // the input tile, later c and d (which need more room than the tile only for K = 1)
-  static constexpr int IN_WORDS = HX * HY * HZ > 2 * HXP * TY * TZ ? HX * HY * HZ : 2 * HXP * TY * TZ;
-  static constexpr int SMEM = (IN_WORDS + 2 * HX * HY * TZ) * (int)sizeof(T);
+  // Shared-memory layout.  INPLACE (TZ <= 2K): the z pass writes a and b over the input tile (a
+  // thread owns its column: all of it is in registers before the writes), c and d follow the
+  // tile, the x pass results go back into the tile.  Otherwise a and b follow the tile and c, d
+  // and the results reuse the tile and a.
+  static constexpr bool INPLACE = 2 * TZ <= HZ;
+  static constexpr int TILE = HX * HY * HZ, PLANE = HX * HY, CD = HXP * TY * TZ;
+  static constexpr int IN_WORDS = INPLACE ? TILE : (TILE > 2 * CD ? TILE : 2 * CD);
+  static constexpr int A_OFF = INPLACE ? 0 : IN_WORDS;
+  static constexpr int B_OFF = A_OFF + PLANE * TZ;
+  static constexpr int C_OFF = INPLACE ? TILE : 0;
+  static constexpr int D_OFF = C_OFF + CD;
+  static constexpr int RES_OFF = INPLACE ? 0 : A_OFF;
+  static constexpr int SMEM = (INPLACE ? TILE + 2 * CD : IN_WORDS + 2 * PLANE * TZ) * (int)sizeof(T);
   static_assert(TXP * TY * TZ <= HX * HY * TZ, "results must fit a");
+  static_assert(!INPLACE || 2 * PLANE * TZ <= TILE, "a, b must fit the tile");
 };
 
 // compile-time loop: f(std::integral_constant<int, I>) for I = B..E-1
@@ -208,18 +221,18 @@ __device__ __forceinline__ void band_row(const T* v, int g, int n, int periodic,
   }
 }
 
-template <int K, class T>
+template <int K, class T, bool SMALL>
 __global__ void __launch_bounds__(256) lattice_apply_kernel(const __grid_constant__ LatParams<T> P,
                                                             const T* __restrict__ src, T* __restrict__ dst,
                                                             const __grid_constant__ PointEpilogue ep) {
-  using G = LatTile<K, T>;
+  using G = LatTile<K, T, SMALL>;
   constexpr int TX = G::TX, TY = G::TY, TZ = G::TZ, HX = G::HX, HY = G::HY, HZ = G::HZ, HXP = G::HXP,
                 TXP = G::TXP, NTH = 256;
   const LatticeMask& m = P.m;
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* in = reinterpret_cast<T*>(smem_raw);  // HX*HY*HZ input tile; later c, d
-  T* a = in + G::IN_WORDS;                 // HX*HY*TZ; later the x pass results
-  T* b = a + HX * HY * TZ;
+  T* in = reinterpret_cast<T*>(smem_raw);  // HX*HY*HZ input tile
+  T* a = in + G::A_OFF;                    // HX*HY*TZ z pass results
+  T* b = in + G::B_OFF;
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY, z0 = blockIdx.z * TZ;
   const int tid = threadIdx.x;
   // tile load: a warp per row of HX nodes, U rows in flight per warp; a lane's (at most two) x
@@ -280,7 +293,15 @@ __global__ void __launch_bounds__(256) lattice_apply_kernel(const __grid_constan
         }
       }
     }
-    if (m.pin_first && tid == 0) {  // node 0 of a singular operator (wherever periodic copies sit)
+    // node 0 of a singular operator (wherever periodic copies of it sit in the tile)
+    bool pin = m.pin_first;
+#pragma unroll
+    for (int dir = 0; dir < 3; ++dir) {
+      const int o = (dir == 0 ? x0 : (dir == 1 ? y0 : z0)) - K, H = dir == 0 ? HX : (dir == 1 ? HY : HZ);
+      const int first = m.periodic[dir] ? ((-o) % m.n[dir] + m.n[dir]) % m.n[dir] : -o;  // tile position of 0
+      pin = pin && first >= 0 && first < H;
+    }
+    if (pin && tid == 0) {
       for (int lz = 0; lz < HZ; ++lz)
         if (lattice_coord(z0 + lz - K, m.n[2], m.periodic[2]) == 0)
           for (int ly = 0; ly < HY; ++ly)
@@ -288,7 +309,7 @@ __global__ void __launch_bounds__(256) lattice_apply_kernel(const __grid_constan
               for (int lx = 0; lx < HX; ++lx)
                 if (lattice_coord(x0 + lx - K, m.n[0], m.periodic[0]) == 0) in[(lz * HY + ly) * HX + lx] = T(0);
     }
-    if (any || m.pin_first) __syncthreads();
+    if (any || pin) __syncthreads();
   }
   // z pass: a = M_z x, b = K_z x on the haloed (x, y) plane
   for (int col = tid; col < HX * HY; col += NTH) {
@@ -304,9 +325,9 @@ __global__ void __launch_bounds__(256) lattice_apply_kernel(const __grid_constan
     });
   }
   __syncthreads();
-  // y pass: c = M_y a, d = K_y a + M_y b on the haloed x range (c, d overwrite the input tile)
-  T* c = in;
-  T* d = in + HXP * TY * TZ;
+  // y pass: c = M_y a, d = K_y a + M_y b on the haloed x range
+  T* c = in + G::C_OFF;
+  T* d = in + G::D_OFF;
   for (int col = tid; col < HX * TZ; col += NTH) {
     const int lx = col % HX, tz = col / HX;
     T va[HY], vb[HY];
@@ -326,7 +347,7 @@ __global__ void __launch_bounds__(256) lattice_apply_kernel(const __grid_constan
   }
   __syncthreads();
   // x pass: a thread per (row, cell segment of K nodes), rows across the lanes
-  T* res = a;
+  T* res = in + G::RES_OFF;
   constexpr int SEG = TX / K, ROWS = TY * TZ;
   for (int it = tid; it < SEG * ROWS; it += NTH) {
     const int row = it % ROWS, q = it / ROWS;
@@ -372,10 +393,10 @@ __global__ void __launch_bounds__(256) lattice_apply_kernel(const __grid_constan
   }
 }
 
-template <int K, class T>
+template <int K, class T, bool SMALL>
 static void launch_apply(const LatticeHost& L, const T* src, T* dst, const PointEpilogue& ep, cudaStream_t s) {
-  using G = LatTile<K, T>;
-  auto kern = lattice_apply_kernel<K, T>;
+  using G = LatTile<K, T, SMALL>;
+  auto kern = lattice_apply_kernel<K, T, SMALL>;
   ensure_smem_attr((const void*)kern, G::SMEM);
   dim3 grid((L.mask.n[0] + G::TX - 1) / G::TX, (L.mask.n[1] + G::TY - 1) / G::TY,
             (L.mask.n[2] + G::TZ - 1) / G::TZ);
@@ -390,12 +411,23 @@ static void launch_apply(const LatticeHost& L, const T* src, T* dst, const Point
   EXG_CUDA(cudaGetLastError());
 }
 
+// full-size tiles of a lattice
+template <int K, class T>
+static long long tiles(const LatticeHost& L) {
+  using G = LatTile<K, T, false>;
+  return (long long)((L.mask.n[0] + G::TX - 1) / G::TX) * ((L.mask.n[1] + G::TY - 1) / G::TY) *
+         ((L.mask.n[2] + G::TZ - 1) / G::TZ);
+}
+
 template <class T>
 static void apply_t(LatticeHost& L, const T* src, T* dst, const PointEpilogue& ep, cudaStream_t s) {
   switch (L.k) {
-#define EXG_LAT_CASE(KK)                     \
-  case KK:                                   \
-    launch_apply<KK, T>(L, src, dst, ep, s); \
+#define EXG_LAT_CASE(KK)                                                    \
+  case KK:                                                                  \
+    if (tiles<KK, T>(L) < 152)                                              \
+      launch_apply<KK, T, true>(L, src, dst, ep, s);                        \
+    else                                                                    \
+      launch_apply<KK, T, false>(L, src, dst, ep, s);                       \
     break;
     EXG_LAT_CASE(1)
     EXG_LAT_CASE(2)
@@ -411,13 +443,109 @@ static void apply_t(LatticeHost& L, const T* src, T* dst, const PointEpilogue& e
   }
 }
 
+// Q1 lattices (every h-level of cphMG): a thread per node evaluates the (2K+1)^3-point stencil
+// from global memory (neighbours are L1/L2 hits) in one launch without the tile pipeline's
+// barriers, which make the tile kernel latency-bound on the small coarse lattices
+__device__ __forceinline__ int wrap_or_out(int g, int n, int periodic) {
+  if (g >= 0 && g < n) return g;
+  if (!periodic) return -1;
+  return ((g % n) + n) % n;
+}
+
+template <int K, class T>
+__global__ void __launch_bounds__(256) lattice_direct_kernel(const __grid_constant__ LatParams<T> P,
+                                                             const T* __restrict__ src, T* __restrict__ dst,
+                                                             const __grid_constant__ PointEpilogue ep) {
+  constexpr int W = 2 * K + 1, B = band_off(K);
+  const LatticeMask& m = P.m;
+  const int total = m.n[0] * m.n[1] * m.n[2];
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int g[3] = {i % m.n[0], (i / m.n[0]) % m.n[1], i / (m.n[0] * m.n[1])};
+    // per direction: neighbour coordinates (-1 outside), their Dirichlet flags, the mass and
+    // stiffness rows of the node's row type (vertex rows at a bounded line's end without the
+    // missing cell's diagonal entry)
+    int nb[3][W];
+    bool fc[3][W];
+    T mm[3][W], kk[3][W];
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int n = m.n[d], per = m.periodic[d], t = g[d] % K;
+#pragma unroll
+      for (int o = 0; o < W; ++o) {
+        const int c = wrap_or_out(g[d] + o - K, n, per);
+        nb[d][o] = c;
+        fc[d][o] = !per && ((c == 0 && m.dirichlet[2 * d]) || (c == n - 1 && m.dirichlet[2 * d + 1]));
+        mm[d][o] = band<T>(B + (0 * K + t) * W + o) * P.hm[d];
+        kk[d][o] = band<T>(B + (1 * K + t) * W + o) * P.hk[d];
+      }
+      if (!per && g[d] == 0) {
+        mm[d][K] -= band<T>(B + 2 * K * W + 0) * P.hm[d];
+        kk[d][K] -= band<T>(B + 2 * K * W + 2) * P.hk[d];
+      }
+      if (!per && g[d] == n - 1) {
+        mm[d][K] -= band<T>(B + 2 * K * W + 1) * P.hm[d];
+        kk[d][K] -= band<T>(B + 2 * K * W + 3) * P.hk[d];
+      }
+    }
+    T acc = T(0);
+#pragma unroll
+    for (int c = 0; c < W; ++c)
+#pragma unroll
+      for (int b = 0; b < W; ++b) {
+        T sx = T(0), tx = T(0);  // sum_a K_x x, sum_a M_x x along the row (b, c)
+        const bool rowok = nb[1][b] >= 0 && nb[2][c] >= 0 && !fc[1][b] && !fc[2][c];
+        const int rbase = m.n[0] * (nb[1][b] + m.n[1] * nb[2][c]);
+#pragma unroll
+        for (int a = 0; a < W; ++a) {
+          const bool ok = rowok && nb[0][a] >= 0 && !fc[0][a] &&
+                          !(m.pin_first && nb[0][a] == 0 && nb[1][b] == 0 && nb[2][c] == 0);
+          const T x = ok ? src[rbase + nb[0][a]] : T(0);
+          sx += kk[0][a] * x;
+          tx += mm[0][a] * x;
+        }
+        acc += sx * mm[1][b] * mm[2][c] + tx * (kk[1][b] * mm[2][c] + mm[1][b] * kk[2][c]);
+      }
+    const bool con = (!m.periodic[0] && ((g[0] == 0 && m.dirichlet[0]) || (g[0] == m.n[0] - 1 && m.dirichlet[1]))) ||
+                     (!m.periodic[1] && ((g[1] == 0 && m.dirichlet[2]) || (g[1] == m.n[1] - 1 && m.dirichlet[3]))) ||
+                     (!m.periodic[2] && ((g[2] == 0 && m.dirichlet[4]) || (g[2] == m.n[2] - 1 && m.dirichlet[5]))) ||
+                     (m.pin_first && i == 0);
+    if (con) acc = src[i];
+    epilogue_store<T>(ep, dst, i, src, acc);
+  }
+}
+
+template <int K, class T>
+static void apply_direct(const LatticeHost& L, const T* src, T* dst, const PointEpilogue& ep, cudaStream_t s) {
+  LatParams<T> P;
+  P.m = L.mask;
+  for (int e = 0; e < 3; ++e) {
+    P.hm[e] = (T)L.h[e];
+    P.hk[e] = (T)(1.0 / L.h[e]);
+  }
+  const long long total = L.size();
+  const int blocks = (int)std::max<long long>(1, std::min<long long>((total + 255) / 256, 152LL * 16));
+  lattice_direct_kernel<K, T><<<blocks, 256, 0, s>>>(P, src, dst, ep);
+  EXG_CUDA(cudaGetLastError());
+}
+
+// the direct kernel for Q1 (measured: at Q2 its 125 loads per node make it slower than the tiles)
+static bool use_direct(const LatticeHost& L) { return L.k == 1; }
+
 void lattice_apply(LatticeHost& L, int precision, const void* src, void* dst, cudaStream_t s,
                    const PointEpilogue& ep) {
   if (precision == EXG_PREC_F32) {
-    apply_t<float>(L, (const float*)src, (float*)dst, ep, s);
+    if (use_direct(L))
+      L.k == 1 ? apply_direct<1, float>(L, (const float*)src, (float*)dst, ep, s)
+               : apply_direct<2, float>(L, (const float*)src, (float*)dst, ep, s);
+    else
+      apply_t<float>(L, (const float*)src, (float*)dst, ep, s);
   } else {
     EXG_CHECK(precision == EXG_PREC_F64, EXG_ERR_UNSUPPORTED, "continuous levels compute in FP32 or FP64");
-    apply_t<double>(L, (const double*)src, (double*)dst, ep, s);
+    if (use_direct(L))
+      L.k == 1 ? apply_direct<1, double>(L, (const double*)src, (double*)dst, ep, s)
+               : apply_direct<2, double>(L, (const double*)src, (double*)dst, ep, s);
+    else
+      apply_t<double>(L, (const double*)src, (double*)dst, ep, s);
   }
 }
 
@@ -527,6 +655,54 @@ __global__ void lattice_pass_kernel(const T* __restrict__ in, T* __restrict__ ou
     } else {
       out[i] = acc;
     }
+  }
+}
+
+// the three passes of a transfer in one kernel when every direction has at most W = 3 taps per
+// row (all transfers of cphMG except the finest continuous p-step): a thread per destination node
+// sums the W^3 products of its three 1D rows (constrained input nodes read as zero), and adds at
+// an unconstrained destination node
+template <class T, int W>
+__global__ void lattice_transfer_direct_kernel(const T* __restrict__ in, T* __restrict__ out, int o0, int o1, int o2,
+                                               int i0, int i1, const int* __restrict__ cx, const T* __restrict__ vx,
+                                               const int* __restrict__ cy, const T* __restrict__ vy,
+                                               const int* __restrict__ cz, const T* __restrict__ vz,
+                                               const __grid_constant__ LatticeMask min,
+                                               const __grid_constant__ LatticeMask mout) {
+  const int total = o0 * o1 * o2;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < total; i += gridDim.x * blockDim.x) {
+    const int x = i % o0, y = (i / o0) % o1, z = i / (o0 * o1);
+    if (dev_constrained(mout, x, y, z)) continue;
+    int ax[W], ay[W], az[W];
+    T wx[W], wy[W], wz[W];
+    bool fx[W], fy[W], fz[W];
+#pragma unroll
+    for (int t = 0; t < W; ++t) {
+      ax[t] = cx[x * W + t];
+      ay[t] = cy[y * W + t];
+      az[t] = cz[z * W + t];
+      wx[t] = vx[x * W + t];
+      wy[t] = vy[y * W + t];
+      wz[t] = vz[z * W + t];
+      fx[t] = !min.periodic[0] && ((ax[t] == 0 && min.dirichlet[0]) || (ax[t] == min.n[0] - 1 && min.dirichlet[1]));
+      fy[t] = !min.periodic[1] && ((ay[t] == 0 && min.dirichlet[2]) || (ay[t] == min.n[1] - 1 && min.dirichlet[3]));
+      fz[t] = !min.periodic[2] && ((az[t] == 0 && min.dirichlet[4]) || (az[t] == min.n[2] - 1 && min.dirichlet[5]));
+    }
+    T acc = T(0);
+#pragma unroll
+    for (int c = 0; c < W; ++c)
+#pragma unroll
+      for (int b = 0; b < W; ++b) {
+        T row = T(0);
+        const int rbase = i0 * (ay[b] + i1 * az[c]);
+#pragma unroll
+        for (int a = 0; a < W; ++a) {
+          const bool zero = fx[a] || fy[b] || fz[c] || (min.pin_first && ax[a] == 0 && ay[b] == 0 && az[c] == 0);
+          row += zero ? T(0) : wx[a] * in[rbase + ax[a]];
+        }
+        acc += wy[b] * wz[c] * row;
+      }
+    out[i] += acc;
   }
 }
 
@@ -736,6 +912,14 @@ static void prolongate_t(const LatticeTransfer& t, const T* coarse, T* fine, cud
     EXG_CUDA(cudaGetLastError());
     return;
   }
+  if (t.wp[0] == 2 && t.wp[1] == 2 && t.wp[2] == 2) {
+    const long long total = (long long)t.mf.n[0] * t.mf.n[1] * t.mf.n[2];
+    lattice_transfer_direct_kernel<T, 2><<<grid_for(total), 256, 0, s>>>(
+        coarse, fine, t.mf.n[0], t.mf.n[1], t.mf.n[2], t.mc.n[0], t.mc.n[1], t.pcol[0], (const T*)t.pval[0], t.pcol[1],
+        (const T*)t.pval[1], t.pcol[2], (const T*)t.pval[2], t.mc, t.mf);
+    EXG_CUDA(cudaGetLastError());
+    return;
+  }
   T* s0 = (T*)t.scratch[0];
   T* s1 = (T*)t.scratch[1];
   const int d0[3] = {t.mf.n[0], t.mc.n[1], t.mc.n[2]};
@@ -751,6 +935,14 @@ static void restrict_t(const LatticeTransfer& t, const T* fine, T* coarse, cudaS
   if (t.to_dg) {
     c_restrict_kernel<T><<<grid_for((long long)t.mc.n[0] * t.mc.n[1] * t.mc.n[2]), 256, 0, s>>>(
         fine, coarse, t.mc, t.Nc[0], t.Nc[1], t.Nc[2], t.kc);
+    EXG_CUDA(cudaGetLastError());
+    return;
+  }
+  if (t.wr[0] == 3 && t.wr[1] == 3 && t.wr[2] == 3) {
+    const long long total = (long long)t.mc.n[0] * t.mc.n[1] * t.mc.n[2];
+    lattice_transfer_direct_kernel<T, 3><<<grid_for(total), 256, 0, s>>>(
+        fine, coarse, t.mc.n[0], t.mc.n[1], t.mc.n[2], t.mf.n[0], t.mf.n[1], t.rcol[0], (const T*)t.rval[0], t.rcol[1],
+        (const T*)t.rval[1], t.rcol[2], (const T*)t.rval[2], t.mf, t.mc);
     EXG_CUDA(cudaGetLastError());
     return;
   }

@@ -64,6 +64,21 @@ def test_continuous_apply_ragged_tiles(n_cells, k, periodic):
     assert rel(d, 1.0 / oc.diagonal()) <= 1e-13
 
 
+@pytest.mark.parametrize("k,n", [(2, 52), (3, 20), (4, 20), (5, 12)])
+@pytest.mark.parametrize("prec", [E.PREC_F64, E.PREC_F32])
+@pytest.mark.parametrize("periodic", [(0, 0, 0), (1, 0, 1)])
+def test_continuous_apply_full_tiles(k, n, prec, periodic):
+    """Lattices large enough for the full-size tiles (and, at k = 2, above the direct kernel's
+    size limit), with the Chebyshev store fused."""
+    torch = require_gpu()
+    kw = dict(n_cells=(n, n, n), periodic=periodic, bc=(0, 1, 0, 0, 1, 0))
+    oc, op = _pair(kw, k, prec, False)
+    x = splitmix_uniform(oc.n_dofs, 31)
+    y = op.vmult(op.initialize_dof_vector(), to_dev(torch, x, op.dtype)).cpu().numpy()
+    ref = oc.apply(x) if prec == E.PREC_F64 else oc.apply_f32(x.astype(np.float32))
+    assert rel(y, ref) <= (1e-13 if prec == E.PREC_F64 else 2e-6)
+
+
 @pytest.mark.parametrize("kind", ["mixed", "periodic"])
 def test_continuous_inverse_diagonal_and_residual(kind):
     torch = require_gpu()

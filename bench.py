@@ -498,13 +498,16 @@ def run_component(args):
     s = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     if args.mode == "operator":
-        op = E.LaplaceOperator(mesh, k, 1.0, precs[args.precision])
-        if op.cartesian and not args.no_tune:
+        if args.continuous:  # the continuous FE_Q operator of cphMG's levels (Cartesian meshes)
+            op = E.ContinuousLaplaceOperator(mesh, k, precision=precs[args.precision])
+        else:
+            op = E.LaplaceOperator(mesh, k, 1.0, precs[args.precision])
+        if op.cartesian and not args.no_tune and not args.continuous:
             op.tune()
         x = torch.tensor(splitmix_uniform(op.n_dofs, 1), device="cuda").to(op.dtype)
         y = torch.empty_like(x)
         run = lambda: op.vmult(y, x)
-        what = {"precision": args.precision}
+        what = {"precision": args.precision, "operator": "continuous FE_Q" if args.continuous else "SIPG DG"}
     else:
         op = E.LaplaceOperator(mesh, k, 1.0, E.PREC_F64E)
         if op.cartesian:
@@ -635,6 +638,7 @@ def main():
     ap.add_argument("--mode", default="apply", choices=["apply", "solve", "sweep", "learned", "operator", "vcycle"])
     ap.add_argument("--curved", action="store_true", help="operator / vcycle modes: deformed-cube mesh")
     ap.add_argument("--mg-type", default="ph", choices=["ph", "cph"], help="vcycle mode: phMG or cphMG")
+    ap.add_argument("--continuous", action="store_true", help="operator mode: the continuous FE_Q operator")
     ap.add_argument("--learned-steps", type=int, default=400)
     ap.add_argument("--learned-epochs", type=int, default=40)
     ap.add_argument("--learned-diagnostics", action="store_true")

@@ -240,12 +240,39 @@ __global__ void __launch_bounds__(256) lattice_apply_kernel(const __grid_constan
   const int lane = tid & 31, warp = tid >> 5;
   static_assert(HX <= 64, "two x positions per lane");
   constexpr int U = sizeof(T) == 4 ? 8 : 4, ROWS_IN = HY * HZ;
+  // tiles whose haloed box lies inside the lattice (most of them) need no wrap or range test
+  const bool interior = x0 >= K && x0 - K + HX <= m.n[0] && y0 >= K && y0 - K + HY <= m.n[1] && z0 >= K &&
+                        z0 - K + HZ <= m.n[2];
+  if (interior) {
+    const T* base = src + ((x0 - K) + m.n[0] * ((y0 - K) + m.n[1] * (z0 - K)));
+    for (int r0 = warp * U; r0 < ROWS_IN; r0 += (NTH / 32) * U) {
+      T vals[U][2];
+#pragma unroll
+      for (int u = 0; u < U; ++u) {
+        const int r = r0 + u;
+        const T* rp = base + m.n[0] * (r % HY + m.n[1] * (r / HY));
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const int lx = lane + 32 * c;
+          vals[u][c] = (r < ROWS_IN && lx < HX) ? rp[lx] : T(0);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < U; ++u)
+#pragma unroll
+        for (int c = 0; c < 2; ++c) {
+          const int lx = lane + 32 * c;
+          if (r0 + u < ROWS_IN && lx < HX) in[(r0 + u) * HX + lx] = vals[u][c];
+        }
+    }
+  }
   int gxs[2];
 #pragma unroll
   for (int c = 0; c < 2; ++c) {
     const int lx = lane + 32 * c;
     gxs[c] = lx < HX ? lattice_coord(x0 + lx - K, m.n[0], m.periodic[0]) : -1;
   }
+  if (!interior)
   for (int r0 = warp * U; r0 < ROWS_IN; r0 += (NTH / 32) * U) {
     T vals[U][2];
 #pragma unroll
@@ -714,18 +741,19 @@ static int padded_width(int w) {
   return 0;
 }
 
-// c-transfer: every DG DoF reads its lattice node
-template <class T>
+// c-transfer: every DG DoF reads its lattice node (K compile-time: the index splits are
+// multiply-shifts)
+template <class T, int K>
 __global__ void c_prolongate_kernel(const T* __restrict__ coarse, T* __restrict__ fine,
-                                    const __grid_constant__ LatticeMask m, int N0, int N1, int N2, int k) {
-  const int n = k + 1, n3 = n * n * n;
+                                    const __grid_constant__ LatticeMask m, int N0, int N1, int N2) {
+  constexpr int n = K + 1, n3 = n * n * n;
   const long long total = (long long)N0 * N1 * N2 * n3;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
     const long long c = i / n3;
-    const int q = (int)(i % n3);
-    int g[3] = {(int)(c % N0) * k + q % n, (int)((c / N0) % N1) * k + (q / n) % n,
-                (int)(c / ((long long)N0 * N1)) * k + q / (n * n)};
+    const int q = (int)(i - c * n3);
+    const int cx = (int)(c % N0), cyz = (int)(c / N0), cy = cyz % N1, cz = cyz / N1;
+    int g[3] = {cx * K + q % n, cy * K + (q / n) % n, cz * K + q / (n * n)};
     for (int d = 0; d < 3; ++d)
       if (m.periodic[d] && g[d] >= m.n[d]) g[d] -= m.n[d];
     if (dev_constrained(m, g[0], g[1], g[2])) continue;
@@ -735,19 +763,21 @@ __global__ void c_prolongate_kernel(const T* __restrict__ coarse, T* __restrict_
 
 // c-transfer restriction: every unconstrained lattice node sums the DG DoFs at its position
 // (one cell in each direction, two at a cell vertex)
-template <class T>
+template <class T, int K>
 __global__ void c_restrict_kernel(const T* __restrict__ fine, T* __restrict__ coarse,
-                                  const __grid_constant__ LatticeMask m, int N0, int N1, int N2, int k) {
-  const int n = k + 1;
+                                  const __grid_constant__ LatticeMask m, int N0, int N1, int N2) {
+  constexpr int n = K + 1;
   const int Nd[3] = {N0, N1, N2};
   const long long total = (long long)m.n[0] * m.n[1] * m.n[2];
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
-    const int g[3] = {(int)(i % m.n[0]), (int)((i / m.n[0]) % m.n[1]), (int)(i / ((long long)m.n[0] * m.n[1]))};
+    const int ii = (int)i;  // lattices have fewer than 2^31 nodes
+    const int g[3] = {ii % m.n[0], (ii / m.n[0]) % m.n[1], ii / (m.n[0] * m.n[1])};
     if (dev_constrained(m, g[0], g[1], g[2])) continue;
     int cell[3][2], loc[3][2], cnt[3];
+#pragma unroll
     for (int d = 0; d < 3; ++d) {
-      const int e = g[d] / k, l = g[d] % k;
+      const int e = g[d] / K, l = g[d] - e * K;
       cnt[d] = 0;
       if (l != 0) {
         cell[d][0] = e;
@@ -757,7 +787,7 @@ __global__ void c_restrict_kernel(const T* __restrict__ fine, T* __restrict__ co
       }
       if (e >= 1 || m.periodic[d]) {  // left cell, its last node
         cell[d][cnt[d]] = e >= 1 ? e - 1 : Nd[d] - 1;
-        loc[d][cnt[d]] = k;
+        loc[d][cnt[d]] = K;
         ++cnt[d];
       }
       if (e < Nd[d]) {  // right cell, its first node
@@ -771,7 +801,7 @@ __global__ void c_restrict_kernel(const T* __restrict__ fine, T* __restrict__ co
       for (int cy = 0; cy < cnt[1]; ++cy)
         for (int cx = 0; cx < cnt[0]; ++cx) {
           const long long c = cell[0][cx] + (long long)N0 * (cell[1][cy] + (long long)N1 * cell[2][cz]);
-          acc += fine[c * n * n * n + loc[0][cx] + n * (loc[1][cy] + n * loc[2][cz])];
+          acc += fine[c * (n * n * n) + loc[0][cx] + n * (loc[1][cy] + n * loc[2][cz])];
         }
     coarse[i] += acc;
   }
@@ -908,7 +938,16 @@ template <class T>
 static void prolongate_t(const LatticeTransfer& t, const T* coarse, T* fine, cudaStream_t s) {
   if (t.to_dg) {
     const long long total = (long long)t.Nc[0] * t.Nc[1] * t.Nc[2] * (t.kc + 1) * (t.kc + 1) * (t.kc + 1);
-    c_prolongate_kernel<T><<<grid_for(total), 256, 0, s>>>(coarse, fine, t.mc, t.Nc[0], t.Nc[1], t.Nc[2], t.kc);
+    switch (t.kc) {
+#define EXG_CP(KK)                                                                                          \
+  case KK:                                                                                                  \
+    c_prolongate_kernel<T, KK><<<grid_for(total), 256, 0, s>>>(coarse, fine, t.mc, t.Nc[0], t.Nc[1], t.Nc[2]); \
+    break;
+      EXG_CP(1) EXG_CP(2) EXG_CP(3) EXG_CP(4) EXG_CP(5) EXG_CP(6) EXG_CP(7) EXG_CP(8)
+#undef EXG_CP
+      default:
+        EXG_CHECK(false, EXG_ERR_UNSUPPORTED, "continuous level degree must be 1..8");
+    }
     EXG_CUDA(cudaGetLastError());
     return;
   }
@@ -933,8 +972,17 @@ static void prolongate_t(const LatticeTransfer& t, const T* coarse, T* fine, cud
 template <class T>
 static void restrict_t(const LatticeTransfer& t, const T* fine, T* coarse, cudaStream_t s) {
   if (t.to_dg) {
-    c_restrict_kernel<T><<<grid_for((long long)t.mc.n[0] * t.mc.n[1] * t.mc.n[2]), 256, 0, s>>>(
-        fine, coarse, t.mc, t.Nc[0], t.Nc[1], t.Nc[2], t.kc);
+    const int g = grid_for((long long)t.mc.n[0] * t.mc.n[1] * t.mc.n[2]);
+    switch (t.kc) {
+#define EXG_CR(KK)                                                                                 \
+  case KK:                                                                                         \
+    c_restrict_kernel<T, KK><<<g, 256, 0, s>>>(fine, coarse, t.mc, t.Nc[0], t.Nc[1], t.Nc[2]); \
+    break;
+      EXG_CR(1) EXG_CR(2) EXG_CR(3) EXG_CR(4) EXG_CR(5) EXG_CR(6) EXG_CR(7) EXG_CR(8)
+#undef EXG_CR
+      default:
+        EXG_CHECK(false, EXG_ERR_UNSUPPORTED, "continuous level degree must be 1..8");
+    }
     EXG_CUDA(cudaGetLastError());
     return;
   }

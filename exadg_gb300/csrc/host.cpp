@@ -75,6 +75,14 @@ std::unique_ptr<exg_op> exg_op::continuous_level(const MeshInfo& m, int deg, int
   op->lat.reset(new LatticeHost());
   make_lattice(m, deg, singular, *op->lat);
   lattice_prepare(*op->lat, prec);
+  if (!op->cartesian) {
+    // curved: the DG geometry with every face read as Neumann is the cell term alone
+    std::vector<long long> neumann((size_t)m.n_cells() * 6, -2);
+    EXG_CUDA(cudaMemcpy(op->geo->fnb, neumann.data(), neumann.size() * sizeof(long long), cudaMemcpyHostToDevice));
+    op->cdg.reset(new DgScratch());
+    const size_t bytes = (size_t)m.n_cells() * op->n * op->n * op->n * psize(prec);
+    for (void*& p : op->cdg->v) p = dalloc(bytes);
+  }
   return op;
 }
 
@@ -84,8 +92,17 @@ void exg_op::apply(const void* src, void* dst, int n_rhs, cudaStream_t s, const 
     EXG_CHECK(cell_begin == 0 && cell_end < 0, EXG_ERR_INVALID, "continuous levels apply on the whole lattice");
     EXG_CHECK(n_rhs == 1 || ep.mode < 0, EXG_ERR_INVALID, "fused store needs a single right-hand side");
     const size_t stride = (size_t)lat->size() * (precision == EXG_PREC_F32 ? 4 : 8);
-    for (int r = 0; r < n_rhs; ++r)
-      lattice_apply(*lat, precision, (const char*)src + r * stride, dst ? (char*)dst + r * stride : nullptr, s, ep);
+    for (int r = 0; r < n_rhs; ++r) {
+      const void* sr = (const char*)src + r * stride;
+      void* dr = dst ? (char*)dst + r * stride : nullptr;
+      if (cartesian) {
+        lattice_apply(*lat, precision, sr, dr, s, ep);
+      } else {
+        lattice_to_dg(*lat, precision, sr, cdg->v[0], s);
+        general_apply(*geo, fe, cdg->v[0], cdg->v[1], 1, s);
+        dg_to_lattice_apply(*lat, precision, cdg->v[1], sr, dr, ep, s);
+      }
+    }
     return;
   }
   const long long nc = mesh.n_cells();
@@ -176,8 +193,12 @@ void exg_op::apply_host(const double* src_host, double* dst_host, int n_slabs, c
 }
 
 void exg_op::diagonal(void* d, bool invert, cudaStream_t s) const {
-  if (continuous)
+  if (continuous && cartesian) {
     lattice_diagonal(*lat, precision, d, invert, s);
+  } else if (continuous) {
+    general_diagonal(*geo, fe, cdg->v[1], false, s);
+    dg_to_lattice_diagonal(*lat, precision, cdg->v[1], d, invert, s);
+  }
   else if (cartesian)
     cart_diagonal(cart, precision, d, invert, s);
   else
@@ -496,8 +517,6 @@ exg_mg::exg_mg(const exg_op& fine, const exg_mg_desc& d) : desc(d) {
   prec = d.mg_precision;
   coarse_prec = d.coarse_double ? EXG_PREC_F64 : prec;
   EXG_CHECK(d.mg_type == EXG_MG_PH || d.mg_type == EXG_MG_CPH, EXG_ERR_INVALID, "mg_type must be EXG_MG_PH or EXG_MG_CPH");
-  EXG_CHECK(d.mg_type == EXG_MG_PH || fine.cartesian, EXG_ERR_UNSUPPORTED,
-            "cphMG (continuous levels) needs a Cartesian mesh");
   auto list = mg_level_list(fine.mesh.N, fine.degree, std::max(1, d.min_coarse_cells), d.mg_type == EXG_MG_CPH);
   EXG_CHECK(list.size() <= 32, EXG_ERR_UNSUPPORTED, "too many levels");
   cudaStream_t s = nullptr;

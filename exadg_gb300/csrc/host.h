@@ -66,6 +66,15 @@ struct exg_op {
   static std::unique_ptr<exg_op> continuous_level(const exg::MeshInfo& m, int degree, int precision, bool singular);
   bool continuous = false;
   std::unique_ptr<exg::LatticeHost> lat;
+  // curved continuous levels: two DG-layout work vectors around the cell-term apply
+  struct DgScratch {
+    void* v[2] = {nullptr, nullptr};
+    ~DgScratch() {
+      for (void* p : v)
+        if (p) cudaFree(p);
+    }
+  };
+  std::unique_ptr<DgScratch> cdg;
   long long n_dofs() const { return continuous ? lat->size() : mesh.n_cells() * n * n * n; }
   // dst = A src on the cells [cell_begin, cell_end) (cell_end < 0: all cells)
   void apply(const void* src, void* dst, int n_rhs, cudaStream_t s,

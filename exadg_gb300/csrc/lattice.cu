@@ -25,7 +25,6 @@
 namespace exg {
 
 void make_lattice(const MeshInfo& m, int k, bool singular, LatticeHost& L) {
-  EXG_CHECK(m.affine(), EXG_ERR_UNSUPPORTED, "continuous multigrid levels need a Cartesian mesh");
   EXG_CHECK(k >= 1 && k <= LAT_KMAX, EXG_ERR_UNSUPPORTED, "continuous level degree must be 1..8");
   L.k = k;
   for (int d = 0; d < 3; ++d) {
@@ -743,7 +742,7 @@ static int padded_width(int w) {
 
 // c-transfer: every DG DoF reads its lattice node (K compile-time: the index splits are
 // multiply-shifts)
-template <class T, int K>
+template <class T, int K, bool SET = false>
 __global__ void c_prolongate_kernel(const T* __restrict__ coarse, T* __restrict__ fine,
                                     const __grid_constant__ LatticeMask m, int N0, int N1, int N2) {
   constexpr int n = K + 1, n3 = n * n * n;
@@ -756,16 +755,25 @@ __global__ void c_prolongate_kernel(const T* __restrict__ coarse, T* __restrict_
     int g[3] = {cx * K + q % n, cy * K + (q / n) % n, cz * K + q / (n * n)};
     for (int d = 0; d < 3; ++d)
       if (m.periodic[d] && g[d] >= m.n[d]) g[d] -= m.n[d];
-    if (dev_constrained(m, g[0], g[1], g[2])) continue;
-    fine[i] += coarse[g[0] + (long long)m.n[0] * (g[1] + (long long)m.n[1] * g[2])];
+    const T v = dev_constrained(m, g[0], g[1], g[2]) ? T(0)
+                                                      : coarse[g[0] + (long long)m.n[0] * (g[1] + (long long)m.n[1] * g[2])];
+    if (SET)
+      fine[i] = v;
+    else
+      fine[i] += v;
   }
 }
 
 // c-transfer restriction: every unconstrained lattice node sums the DG DoFs at its position
-// (one cell in each direction, two at a cell vertex)
-template <class T, int K>
+// (one cell in each direction, two at a cell vertex).  MODE 0: coarse += sum (the transfer);
+// MODE 1: the continuous operator on a curved mesh, t = sum of the cell terms, src on constrained
+// nodes, stored through the point epilogue; MODE 2: the diagonal (1 on constrained nodes,
+// inverted when asked)
+template <class T, int K, int MODE = 0>
 __global__ void c_restrict_kernel(const T* __restrict__ fine, T* __restrict__ coarse,
-                                  const __grid_constant__ LatticeMask m, int N0, int N1, int N2) {
+                                  const __grid_constant__ LatticeMask m, int N0, int N1, int N2,
+                                  const T* __restrict__ src = nullptr, PointEpilogue ep = PointEpilogue(),
+                                  int invert = 0) {
   constexpr int n = K + 1;
   const int Nd[3] = {N0, N1, N2};
   const long long total = (long long)m.n[0] * m.n[1] * m.n[2];
@@ -773,7 +781,11 @@ __global__ void c_restrict_kernel(const T* __restrict__ fine, T* __restrict__ co
        i += (long long)gridDim.x * blockDim.x) {
     const int ii = (int)i;  // lattices have fewer than 2^31 nodes
     const int g[3] = {ii % m.n[0], (ii / m.n[0]) % m.n[1], ii / (m.n[0] * m.n[1])};
-    if (dev_constrained(m, g[0], g[1], g[2])) continue;
+    if (dev_constrained(m, g[0], g[1], g[2])) {
+      if (MODE == 1) epilogue_store<T>(ep, coarse, i, src, src[i]);
+      if (MODE == 2) coarse[i] = T(1);
+      continue;
+    }
     int cell[3][2], loc[3][2], cnt[3];
 #pragma unroll
     for (int d = 0; d < 3; ++d) {
@@ -803,7 +815,9 @@ __global__ void c_restrict_kernel(const T* __restrict__ fine, T* __restrict__ co
           const long long c = cell[0][cx] + (long long)N0 * (cell[1][cy] + (long long)N1 * cell[2][cz]);
           acc += fine[c * (n * n * n) + loc[0][cx] + n * (loc[1][cy] + n * loc[2][cz])];
         }
-    coarse[i] += acc;
+    if (MODE == 0) coarse[i] += acc;
+    if (MODE == 1) epilogue_store<T>(ep, coarse, i, src, acc);
+    if (MODE == 2) coarse[i] = invert ? (fabs((double)acc) > 1e-10 ? T(1) / acc : T(1)) : acc;
   }
 }
 
@@ -1016,6 +1030,65 @@ void LatticeTransfer::restrict_add(const void* fine, void* coarse, cudaStream_t 
     restrict_t<float>(*this, (const float*)fine, (float*)coarse, s);
   else
     restrict_t<double>(*this, (const double*)fine, (double*)coarse, s);
+}
+
+// ------------------------------------------------------------------------------------------
+// curved continuous levels: the lattice and the DG layout of the same mesh and degree
+// ------------------------------------------------------------------------------------------
+template <class T>
+static void to_dg_t(const LatticeHost& L, const T* lat, T* dg, cudaStream_t s) {
+  const long long total = (long long)L.N[0] * L.N[1] * L.N[2] * (L.k + 1) * (L.k + 1) * (L.k + 1);
+  switch (L.k) {
+#define EXG_TD(KK)                                                                                              \
+  case KK:                                                                                                      \
+    c_prolongate_kernel<T, KK, true><<<grid_for(total), 256, 0, s>>>(lat, dg, L.mask, L.N[0], L.N[1], L.N[2]); \
+    break;
+    EXG_TD(1) EXG_TD(2) EXG_TD(3) EXG_TD(4) EXG_TD(5) EXG_TD(6) EXG_TD(7) EXG_TD(8)
+#undef EXG_TD
+    default:
+      EXG_CHECK(false, EXG_ERR_UNSUPPORTED, "continuous level degree must be 1..8");
+  }
+  EXG_CUDA(cudaGetLastError());
+}
+
+template <class T, int MODE>
+static void from_dg_t(const LatticeHost& L, const T* dg, const T* src, T* out, const PointEpilogue& ep, bool invert,
+                      cudaStream_t s) {
+  const int g = grid_for(L.size());
+  switch (L.k) {
+#define EXG_FD(KK)                                                                                               \
+  case KK:                                                                                                       \
+    c_restrict_kernel<T, KK, MODE><<<g, 256, 0, s>>>(dg, out, L.mask, L.N[0], L.N[1], L.N[2], src, ep, invert ? 1 : 0); \
+    break;
+    EXG_FD(1) EXG_FD(2) EXG_FD(3) EXG_FD(4) EXG_FD(5) EXG_FD(6) EXG_FD(7) EXG_FD(8)
+#undef EXG_FD
+    default:
+      EXG_CHECK(false, EXG_ERR_UNSUPPORTED, "continuous level degree must be 1..8");
+  }
+  EXG_CUDA(cudaGetLastError());
+}
+
+void lattice_to_dg(const LatticeHost& L, int precision, const void* lat, void* dg, cudaStream_t s) {
+  if (precision == EXG_PREC_F32)
+    to_dg_t<float>(L, (const float*)lat, (float*)dg, s);
+  else
+    to_dg_t<double>(L, (const double*)lat, (double*)dg, s);
+}
+
+void dg_to_lattice_apply(const LatticeHost& L, int precision, const void* dg, const void* src, void* dst,
+                         const PointEpilogue& ep, cudaStream_t s) {
+  if (precision == EXG_PREC_F32)
+    from_dg_t<float, 1>(L, (const float*)dg, (const float*)src, (float*)dst, ep, false, s);
+  else
+    from_dg_t<double, 1>(L, (const double*)dg, (const double*)src, (double*)dst, ep, false, s);
+}
+
+void dg_to_lattice_diagonal(const LatticeHost& L, int precision, const void* dg, void* diag, bool invert,
+                            cudaStream_t s) {
+  if (precision == EXG_PREC_F32)
+    from_dg_t<float, 2>(L, (const float*)dg, nullptr, (float*)diag, PointEpilogue(), invert, s);
+  else
+    from_dg_t<double, 2>(L, (const double*)dg, nullptr, (double*)diag, PointEpilogue(), invert, s);
 }
 
 }  // namespace exg

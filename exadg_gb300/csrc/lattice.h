@@ -53,6 +53,18 @@ void lattice_diagonal(LatticeHost& L, int precision, void* diag, bool invert, cu
 // stream capture)
 void lattice_prepare(LatticeHost& L, int precision);
 
+// Curved meshes: the continuous operator is the DG operator's cell term (a GeneralGeom whose faces
+// all read as Neumann) between a masked gather of the lattice into the DG layout and a sum back
+// per node.  lattice_to_dg: dg = gather(lat), constrained nodes as zero.  dg_to_lattice_apply:
+// t = sum of the DG entries at each node, src on constrained nodes, stored through the point
+// epilogue.  dg_to_lattice_diagonal: the same sum of the cell-term diagonals, 1 on constrained
+// nodes, optionally inverted.
+void lattice_to_dg(const LatticeHost& L, int precision, const void* lat, void* dg, cudaStream_t s);
+void dg_to_lattice_apply(const LatticeHost& L, int precision, const void* dg, const void* src, void* dst,
+                         const PointEpilogue& ep, cudaStream_t s);
+void dg_to_lattice_diagonal(const LatticeHost& L, int precision, const void* dg, void* diag, bool invert,
+                            cudaStream_t s);
+
 // transfer between level l-1 (continuous) and level l (continuous, or the discontinuous level of
 // the same mesh and degree: the c-transfer)
 struct LatticeTransfer {

@@ -1038,7 +1038,6 @@ struct Lattice {
 };
 
 static Lattice make_lattice(const orc_mesh_desc& m, int k, bool singular) {
-  if (m.deform_amp != 0.0) throw std::runtime_error("continuous levels need a Cartesian (affine box) mesh");
   Lattice L;
   L.k = k;
   for (int d = 0; d < 3; ++d) {
@@ -1115,14 +1114,25 @@ static void band_apply(const Band1D& B, int dir, const int dims[3], const Number
   }
 }
 
+// On a curved mesh (deformed cube) the same operator is the DG operator's cell term assembled
+// through the lattice: gather the cell's nodes, (grad v, grad u) on the cell with its MappingQ
+// geometry and k+1 Gauss points, sum into the nodes.
 template <class Number>
 struct ContinuousLaplace : LevelOp<Number> {
   Lattice L;
   Band1D M[3], K[3];
+  std::unique_ptr<Laplace<Number>> cell;  // curved meshes: the cell term of the DG operator
+  std::vector<long> map;                  // curved meshes: lattice node of each DG DoF
   long n_dofs() const override { return L.size(); }
 
   void init(const orc_mesh_desc& m, int degree, bool singular) {
     L = make_lattice(m, degree, singular);
+    if (m.deform_amp != 0.0) {
+      cell.reset(new Laplace<Number>());
+      cell->init(make_geometry(make_mesh(m), degree + 1), degree, 1.0);
+      dg_map(map);
+      return;
+    }
     for (int d = 0; d < 3; ++d) {
       std::vector<double> Me, Ke;
       element_matrices_1d(degree, L.h[d], Me, Ke);
@@ -1131,8 +1141,41 @@ struct ContinuousLaplace : LevelOp<Number> {
     }
   }
 
+  // curved meshes: per cell f(u_cell) (the cell term, or its diagonal), summed into the nodes
+  template <class F>
+  void assemble(F&& f, std::vector<Number>& y) const {
+    const long nc = cell->n_cells(), n3 = (long)(L.k + 1) * (L.k + 1) * (L.k + 1);
+    std::vector<Number> dg(nc * n3);
+#pragma omp parallel
+    {
+      std::vector<Number> buf(cell->buf_size()), out(n3);
+#pragma omp for schedule(static)
+      for (long c = 0; c < nc; ++c) {
+        f(c, out.data(), buf.data());
+        std::copy(out.begin(), out.end(), dg.begin() + c * n3);
+      }
+    }
+    y.assign(L.size(), Number(0));
+    for (long i = 0; i < (long)map.size(); ++i) y[map[i]] += dg[i];
+  }
+
   void apply(const Number* src, Number* dst) const override {
     long N = L.size();
+    if (cell) {
+      std::vector<Number> x(N), y;
+      for (long i = 0; i < N; ++i) x[i] = L.constrained(i) ? Number(0) : src[i];
+      const long n3 = (long)(L.k + 1) * (L.k + 1) * (L.k + 1);
+      assemble(
+          [&](long c, Number* out, Number* buf) {
+            std::vector<Number> u(n3);
+            for (long q = 0; q < n3; ++q) u[q] = x[map[c * n3 + q]];
+            std::fill(out, out + n3, Number(0));
+            cell->cell_term(c, u.data(), out, buf);
+          },
+          y);
+      for (long i = 0; i < N; ++i) dst[i] = L.constrained(i) ? src[i] : y[i];
+      return;
+    }
     std::vector<Number> x(N), a(N), b(N), c(N), d(N), t(N);
     for (long i = 0; i < N; ++i) x[i] = L.constrained(i) ? Number(0) : src[i];
     band_apply(M[2], 2, L.n, x.data(), a.data());
@@ -1156,6 +1199,24 @@ struct ContinuousLaplace : LevelOp<Number> {
   }
 
   void diagonal(Number* diag) const override {
+    if (cell) {  // sum over the cells at a node of the cell term's diagonal entry
+      const long n3 = (long)(L.k + 1) * (L.k + 1) * (L.k + 1);
+      std::vector<Number> y;
+      assemble(
+          [&](long c, Number* out, Number* buf) {
+            std::vector<Number> e(n3, Number(0)), col(n3);
+            for (long j = 0; j < n3; ++j) {
+              e[j] = Number(1);
+              std::fill(col.begin(), col.end(), Number(0));
+              cell->cell_term(c, e.data(), col.data(), buf);
+              out[j] = col[j];
+              e[j] = Number(0);
+            }
+          },
+          y);
+      for (long i = 0; i < L.size(); ++i) diag[i] = L.constrained(i) ? Number(1) : y[i];
+      return;
+    }
     for (long i = 0; i < L.size(); ++i) {
       int g[3] = {(int)(i % L.n[0]), (int)((i / L.n[0]) % L.n[1]), (int)(i / ((long)L.n[0] * L.n[1]))};
       if (L.constrained(g[0], g[1], g[2])) {

@@ -101,11 +101,8 @@ def test_continuous_operator_rejects_dg_only_calls():
         op.quadrature_points()
     with pytest.raises(E.ExgError):
         E.MultigridPreconditioner(op)
-    curved = E.Mesh(**mesh_kwargs("curved", 2))
     with pytest.raises(E.ExgError):
-        E.ContinuousLaplaceOperator(curved, 2)
-    with pytest.raises(E.ExgError):
-        E.MultigridPreconditioner(E.LaplaceOperator(curved, 2), mg_type=E.MG_CPH)
+        E.MultigridPreconditioner(op, mg_type=7)
 
 
 def sine(k, n=8):
@@ -189,3 +186,64 @@ def test_cphmg_singular_periodic_solve():
     assert abs(its - ro.iterations) <= 1, (its, ro.iterations)
     xg = x.cpu().numpy()
     assert rel(xg - xg.mean(), xo - xo.mean()) <= 1e-8
+
+
+# ---- curved meshes: the continuous operator is the DG cell term assembled through the lattice
+
+
+@pytest.mark.parametrize("k", [1, 2, 3, 5])
+@pytest.mark.parametrize("prec", [E.PREC_F64, E.PREC_F32])
+def test_curved_continuous_apply_and_diagonal(k, prec):
+    torch = require_gpu()
+    kw = mesh_kwargs("curved", 3)
+    oc, op = _pair(kw, k, prec, False)
+    x = splitmix_uniform(oc.n_dofs, 41)
+    y = op.vmult(op.initialize_dof_vector(), to_dev(torch, x, op.dtype)).cpu().numpy()
+    d = op.calculate_inverse_diagonal(op.initialize_dof_vector()).cpu().numpy()
+    if prec == E.PREC_F64:
+        assert rel(y, oc.apply(x)) <= 1e-12
+        assert rel(d, 1.0 / oc.diagonal()) <= 1e-12
+    else:
+        assert rel(y, oc.apply_f32(x.astype(np.float32))) <= 2e-5
+        assert rel(d, 1.0 / oc.diagonal()) <= 2e-5
+    c = oc.constrained()
+    assert np.array_equal(y[c], x.astype(y.dtype)[c])
+
+
+def curved_sine(k, n=8):
+    kw = dict(n_cells=(n, n, n), lo=(-1, -1, -1), hi=(1, 1, 1), bc=(0, 1, 0, 0, 0, 0), deform_amp=0.15,
+              deform_freq=2, deform_left=-1.0, deform_right=1.0, mapping_degree=3)
+    return O.Problem(O.mesh_desc(**kw), k), E.Mesh(**kw)
+
+
+@pytest.mark.parametrize("k", [2, 3])
+def test_curved_cphmg_vcycle_matches_oracle(k):
+    torch = require_gpu()
+    p, m = curved_sine(k, n=4)
+    op = E.LaplaceOperator(m, k)
+    mg = E.MultigridPreconditioner(op, mg_precision=E.PREC_F64, mg_type=E.MG_CPH)
+    omg = O.Multigrid(p, mg_float=0, mg_type=1)
+    assert [g["dg"] for g in mg.info()["levels"]] == [o["dg"] for o in omg.levels()]
+    for seed in (1, 2):
+        r = splitmix_uniform(p.n_dofs, seed)
+        z = mg.vmult(op.initialize_dof_vector(), to_dev(torch, r))
+        assert rel(z.cpu().numpy(), omg.vmult(r)) <= 1e-9
+
+
+@pytest.mark.parametrize("k", [2, 3, 5])
+@pytest.mark.parametrize("mg_prec", [E.PREC_F64, E.PREC_F32])
+def test_curved_cphmg_sine_solve_golden_and_iterations(k, mg_prec):
+    """The reference's curvilinear sine configuration (cphMG, MappingQ3, 8^3 cells)."""
+    torch = require_gpu()
+    p, m = curved_sine(k)
+    op = E.LaplaceOperator(m, k)
+    mg = E.MultigridPreconditioner(op, mg_precision=mg_prec, mg_type=E.MG_CPH)
+    b = p.rhs(O.FN_SINE, 3 * np.pi)
+    x = op.initialize_dof_vector()
+    its = E.KrylovSolver(op, mg).solve(x, to_dev(torch, b))
+    xo, ro = O.Multigrid(p, mg_float=1 if mg_prec == E.PREC_F32 else 0, mg_type=1).solve(b)
+    assert abs(its - ro.iterations) <= 1, (its, ro.iterations)
+    err = p.error(x.cpu().numpy(), O.FN_SINE, 3 * np.pi)
+    gold = GOLD["curvilinear"]["relative_l2_error"][k - 1]
+    assert abs(err - gold) <= 5e-6 * gold
+

@@ -7,7 +7,7 @@ import pytest
 import oracle as O
 from tests.helpers import mesh_kwargs, splitmix_uniform
 
-KINDS = ["dirichlet", "mixed", "periodic", "partial_periodic", "anisotropic"]
+KINDS = ["dirichlet", "mixed", "periodic", "partial_periodic", "anisotropic", "curved"]
 
 
 def _singular(kind):
@@ -46,7 +46,7 @@ def test_galerkin_identity_with_dg_operator(kind, k):
     assert np.allclose(yv[free], cg.apply(v * free)[free], rtol=0, atol=1e-12 * np.abs(yv).max())
 
 
-@pytest.mark.parametrize("kind", ["mixed", "periodic", "partial_periodic"])
+@pytest.mark.parametrize("kind", ["mixed", "periodic", "partial_periodic", "curved"])
 @pytest.mark.parametrize("k", [1, 3])
 def test_diagonal_and_symmetry(kind, k):
     m = O.mesh_desc(**mesh_kwargs(kind, 2))
@@ -146,7 +146,7 @@ def test_cphmg_levels():
     assert [(l["n_cells"][0], l["degree"], l["dg"]) for l in lv1] == [(2, 1, False), (4, 1, False), (4, 1, True)]
 
 
-@pytest.mark.parametrize("kind,k", [("mixed", 3), ("periodic", 2), ("dirichlet", 4)])
+@pytest.mark.parametrize("kind,k", [("mixed", 3), ("periodic", 2), ("dirichlet", 4), ("curved", 3)])
 @pytest.mark.parametrize("mg_float", [0, 1])
 def test_cphmg_solve_matches_phmg_solution(kind, k, mg_float):
     m = O.mesh_desc(**mesh_kwargs(kind, 4))

@@ -471,6 +471,18 @@ def run_solve(args):
                          "speedup": r64["wall_seconds"] / rm["wall_seconds"],
                          "fp32_apply_rel_err_vs_fp64": apply_err,
                          "solution_rel_diff": float(torch.linalg.norm(xm - x64) / torch.linalg.norm(x64))}
+        del o64, o32, y64, y32, v, xm
+        # cphMG: the reference's multigrid for its curvilinear sine test
+        xc64, rc64 = D.solve_unit_cube_sine(nc, kc, E.PREC_F64, E.PREC_F64, curved=True, mg_type=E.MG_CPH)
+        del xc64
+        xcm, rcm = D.solve_unit_cube_sine(nc, kc, E.PREC_F64E, E.PREC_F32, curved=True, mg_type=E.MG_CPH)
+        out["curved_cphmg"] = {
+            "levels": rcm["levels"],
+            "plain_fp64": {kk: rc64[kk] for kk in ("iterations", "wall_seconds", "setup_seconds", "rn", "r0")},
+            "mixed": {kk: rcm[kk] for kk in ("iterations", "wall_seconds", "setup_seconds", "rn", "r0")},
+            "speedup_vs_plain_fp64_phmg": r64["wall_seconds"] / rcm["wall_seconds"],
+            "speedup_vs_mixed_phmg": rm["wall_seconds"] / rcm["wall_seconds"],
+            "solution_rel_diff": float(torch.linalg.norm(xcm - x64) / torch.linalg.norm(x64))}
     line = {"metric": "time to 1e-10 relative residual, mixed (FP32 graph V-cycle) vs plain FP64 CG+MG",
             "value": out["cartesian"]["mixed"]["wall_seconds"], "unit": "s", "higher_is_better": False,
             "mode": "solve", "data": "synthetic (manufactured sine solution)", "configs": out}

@@ -397,7 +397,7 @@ class LaplaceOperator:
 
 
 class ContinuousLaplaceOperator(LaplaceOperator):
-    """Continuous Laplace operator on FE_Q(degree) of a Cartesian mesh, as on the continuous
+    """Continuous Laplace operator on FE_Q(degree), as on the continuous
     levels of cphMG (LaplaceOperator with a continuous DoFHandler): DoFs are the lattice nodes
     (N_d * degree + 1 per direction, N_d * degree when periodic, x fastest); constrained DoFs
     (Dirichlet sides, DoF 0 when singular) keep dst = src."""
@@ -410,7 +410,7 @@ class MultigridPreconditioner:
     """phMG / cphMG V-cycle preconditioner (MultigridPreconditionerBase::vmult).
 
     mg_type: MG_PH (DG on every level) or MG_CPH (continuous FE_Q levels below the finest DG
-    level, the reference's default for the sine and Taylor-Green applications; Cartesian meshes)."""
+    level, the reference's default for the sine and Taylor-Green applications)."""
 
     def __init__(self, operator, mg_precision=PREC_F32, cheb_degree=5, smoothing_range=20.0, eig_iters=20,
                  coarse_rel_tol=1e-3, coarse_abs_tol=1e-12, coarse_max_iter=10000, coarse_double=False,

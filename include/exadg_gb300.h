@@ -65,8 +65,8 @@ exg_status exg_mesh_destroy(exg_mesh* mesh);
  * (Poisson::LaplaceOperator::initialize, poisson/spatial_discretization/laplace_operator.cpp:33-51;
  *  penalty IP::calculate_penalty_parameter, operators/interior_penalty_parameter.h:45-97). */
 exg_status exg_sipg_create(const exg_mesh* mesh, int degree, double ip_factor, int precision, exg_op** op);
-/* Continuous Laplace operator on FE_Q(degree) (Gauss-Lobatto support points) of a Cartesian
- * mesh, as on the continuous levels of cphMG: cell integrals with QGauss(degree+1), constrained
+/* Continuous Laplace operator on FE_Q(degree) (Gauss-Lobatto support points), as on the
+ * continuous levels of cphMG: cell integrals with QGauss(degree+1), constrained
  * DoFs (Dirichlet sides; DoF 0 when singular != 0) keep dst = src
  * (LaplaceOperator with a continuous DoFHandler, laplace_operator.cpp:387-436;
  *  OperatorBase::apply, operators/operator_base.cpp:264-310; multigrid/constraints.h:130-197).
@@ -146,8 +146,7 @@ typedef struct {
   int mg_type;             /* EXG_MG_PH (0): DG on every level (phMG); EXG_MG_CPH (1): cphMG, a
                             * continuous FE_Q(k) level below the finest DG level and coarsening in
                             * the continuous space (multigrid_preconditioner_base.cpp:188-199;
-                            * the default of applications/poisson/sine/application.h:167).
-                            * Continuous levels need a Cartesian mesh. */
+                            * the default of applications/poisson/sine/application.h:167). */
 } exg_mg_desc;
 
 #define EXG_MG_PH 0

@@ -18,6 +18,7 @@ struct GeneralGeom {
   double* face_raw = nullptr;   // optional [cells][6][nq^2][16] Jinv, n, JxW, x
   double* tau = nullptr;        // [cells] surface / volume
   int* bc_dev = nullptr;
+  bool cell_only = false;       // apply the cell term alone (faces all read as Neumann)
   ~GeneralGeom();
   void build(const MeshInfo& m, const FE1D& fe, double ip, int precision, bool keep_raw, cudaStream_t s);
 };

@@ -79,6 +79,7 @@ std::unique_ptr<exg_op> exg_op::continuous_level(const MeshInfo& m, int deg, int
     // curved: the DG geometry with every face read as Neumann is the cell term alone
     std::vector<long long> neumann((size_t)m.n_cells() * 6, -2);
     EXG_CUDA(cudaMemcpy(op->geo->fnb, neumann.data(), neumann.size() * sizeof(long long), cudaMemcpyHostToDevice));
+    op->geo->cell_only = true;
     op->cdg.reset(new DgScratch());
     const size_t bytes = (size_t)m.n_cells() * op->n * op->n * op->n * psize(prec);
     for (void*& p : op->cdg->v) p = dalloc(bytes);

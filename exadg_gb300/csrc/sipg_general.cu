@@ -347,7 +347,8 @@ __host__ __device__ constexpr int gen_cell_stride() { return gen_pad<N, C>(N * N
 template <int N, class C>
 __host__ __device__ constexpr int gen_face_stride() { return gen_pad<N, C>(28 * N * N); }
 
-template <int N, int CPB, class T, class C>
+// FACES = false: the cell term alone (the continuous levels of cphMG on curved meshes)
+template <int N, int CPB, class T, class C, bool FACES = true>
 __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restrict__ src, T* __restrict__ dst,
                                                               const __grid_constant__ GenCoef<N, C> P,
                                                               const C* __restrict__ cellG, const C* __restrict__ face,
@@ -521,7 +522,7 @@ __global__ void __launch_bounds__(CPB* N* N) gen_apply_kernel(const T* __restric
   C* F = fsh + lc * SF;
   const int p1 = a, p2 = b;  // this thread's face point / node
 #pragma unroll 1
-  for (int d = 0; d < 3; ++d) {
+  for (int d = 0; d < (FACES ? 3 : 0); ++d) {
     int t1d, t2d;
     tang(d, t1d, t2d);
     const long long nbs[2] = {active ? fnb[c * 6 + 2 * d] : -2, active ? fnb[c * 6 + 2 * d + 1] : -2};
@@ -806,8 +807,10 @@ static void gen_apply_n(const GeneralGeom& g, const FE1D& fe, const void* src, v
                         const PointEpilogue& ep, long long cb, long long ce) {
   constexpr int CPB = gen_cpb<N>(), N3 = N * N * N, N2 = N * N;
   GenCoef<N, C> P = gen_coef<N, C>(fe);
-  size_t smem = (5 * (size_t)CPB * gen_cell_stride<N, C>() + (size_t)CPB * gen_face_stride<N, C>()) * sizeof(C);
-  auto kern = gen_apply_kernel<N, CPB, T, C>;
+  const bool faces = !g.cell_only;
+  size_t smem = (5 * (size_t)CPB * gen_cell_stride<N, C>() + (faces ? (size_t)CPB * gen_face_stride<N, C>() : 0)) *
+                sizeof(C);
+  auto kern = faces ? gen_apply_kernel<N, CPB, T, C, true> : gen_apply_kernel<N, CPB, T, C, false>;
   ensure_smem_attr((const void*)kern, (int)smem);
   long long blocks = (ce - cb + CPB - 1) / CPB;
   dim3 grid((unsigned)blocks, (unsigned)n_rhs);

@@ -119,7 +119,9 @@ EXPORTED_SYMBOLS = [
     "exg_sipg_info", "exg_sipg_tune", "exg_sipg_set_launch_config", "exg_sipg_apply_f64", "exg_sipg_apply_f32",
     "exg_sipg_residual_f64", "exg_sipg_apply_host_f64", "exg_sipg_inverse_diagonal_f64",
     "exg_sipg_inverse_diagonal_f32", "exg_sipg_quadrature_points", "exg_sipg_rhs", "exg_mg_default_desc",
-    "exg_mg_create", "exg_mg_destroy", "exg_mg_vmult", "exg_mg_info_get", "exg_mg_level_timings", "exg_cg_default_desc", "exg_cg_solve",
+    "exg_mg_create", "exg_mg_destroy", "exg_mg_vmult", "exg_mg_info_get", "exg_mg_level_timings",
+    "exg_mg_level_n_dofs", "exg_mg_level_apply", "exg_mg_smooth", "exg_mg_restrict_add", "exg_mg_prolongate_add",
+    "exg_mg_coarse_solve", "exg_cg_default_desc", "exg_cg_solve",
     "exg_cg_solve_noalloc", "exg_device_fma_peaks", "exg_status_string", "exg_last_error",
     "exg_cnn_create", "exg_cnn_destroy", "exg_cnn_n_params", "exg_cnn_params", "exg_cnn_forward",
     "exg_cnn_backward", "exg_cnn_train_step", "exg_cnn_adam", "exg_cnn_optimizer_state", "exg_dg_pack", "exg_dg_unpack_add", "exg_dg_pack_diff",
@@ -166,6 +168,12 @@ def load_library(path=LIB_PATH):
         "exg_mg_vmult": [P, P, P, P],
         "exg_mg_info_get": [P, ctypes.POINTER(MGInfo)],
         "exg_mg_level_timings": [P, P, P, ctypes.POINTER(ctypes.c_float), I, ctypes.POINTER(I), P],
+        "exg_mg_level_n_dofs": [P, I, ctypes.POINTER(LL), ctypes.POINTER(I)],
+        "exg_mg_level_apply": [P, I, P, P, P],
+        "exg_mg_smooth": [P, I, P, P, I, P],
+        "exg_mg_restrict_add": [P, I, P, P, P],
+        "exg_mg_prolongate_add": [P, I, P, P, P],
+        "exg_mg_coarse_solve": [P, P, P, P],
         "exg_cg_default_desc": [ctypes.POINTER(CGDesc)],
         "exg_cg_solve": [P, P, ctypes.POINTER(CGDesc), P, P, ctypes.POINTER(CGResult), P],
         "exg_cg_solve_noalloc": [P, ctypes.POINTER(CGDesc), P, P, ctypes.POINTER(CGResult), P],
@@ -460,6 +468,48 @@ class MultigridPreconditioner:
         nl = ctypes.c_int()
         _check(_lib.exg_mg_level_timings(self.h, _ptr(src), _ptr(dst), buf, 32, ctypes.byref(nl), _stream(stream)))
         return [float(buf[i]) for i in range(nl.value)]
+
+    # ---- the level objects (SmootherBase, MultigridTransferBase, CoarseGridSolverBase, level vmult)
+    @property
+    def level_dtype(self):
+        import torch
+
+        return torch.float32 if self.desc.mg_precision == PREC_F32 else torch.float64
+
+    def level_n_dofs(self, level):
+        n = ctypes.c_longlong()
+        dg = ctypes.c_int()
+        _check(_lib.exg_mg_level_n_dofs(self.h, level, ctypes.byref(n), ctypes.byref(dg)))
+        return n.value
+
+    def _lvec(self, t, level, what):
+        return _sized(t, self.level_n_dofs(level), self.level_dtype, what)
+
+    def level_vmult(self, level, dst, src, stream=None):
+        _check(_lib.exg_mg_level_apply(self.h, level, _ptr(self._lvec(src, level, "src")),
+                                       _ptr(self._lvec(dst, level, "dst")), _stream(stream)))
+        return dst
+
+    def smooth(self, level, x, rhs, zero_start, stream=None):
+        """Chebyshev smoother of a level: vmult (zero_start) or step (x updated in place)."""
+        _check(_lib.exg_mg_smooth(self.h, level, _ptr(self._lvec(rhs, level, "rhs")), _ptr(self._lvec(x, level, "x")),
+                                  int(zero_start), _stream(stream)))
+        return x
+
+    def restrict_and_add(self, level, coarse, fine, stream=None):
+        _check(_lib.exg_mg_restrict_add(self.h, level, _ptr(self._lvec(fine, level, "fine")),
+                                        _ptr(self._lvec(coarse, level - 1, "coarse")), _stream(stream)))
+        return coarse
+
+    def prolongate_and_add(self, level, fine, coarse, stream=None):
+        _check(_lib.exg_mg_prolongate_add(self.h, level, _ptr(self._lvec(coarse, level - 1, "coarse")),
+                                          _ptr(self._lvec(fine, level, "fine")), _stream(stream)))
+        return fine
+
+    def coarse_solve(self, dst, src, stream=None):
+        _check(_lib.exg_mg_coarse_solve(self.h, _ptr(self._lvec(src, 0, "src")), _ptr(self._lvec(dst, 0, "dst")),
+                                        _stream(stream)))
+        return dst
 
     def info(self):
         i = MGInfo()

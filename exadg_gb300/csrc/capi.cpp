@@ -257,6 +257,50 @@ exg_status exg_mg_level_timings(exg_mg* mg, const double* src, double* dst, floa
   EXG_API_END
 }
 
+exg_status exg_mg_level_n_dofs(const exg_mg* mg, int level, long long* n_dofs, int* is_dg) {
+  EXG_API_BEGIN
+  EXG_CHECK(mg && n_dofs, EXG_ERR_INVALID, "null argument");
+  EXG_CHECK(level >= 0 && level < (int)mg->lv.size(), EXG_ERR_INVALID, "level out of range");
+  *n_dofs = mg->lv[level].n;
+  if (is_dg) *is_dg = mg->lv[level].dg;
+  EXG_API_END
+}
+
+exg_status exg_mg_level_apply(exg_mg* mg, int level, const void* src, void* dst, void* stream) {
+  EXG_API_BEGIN
+  EXG_CHECK(mg && src && dst && src != dst, EXG_ERR_INVALID, "null or aliased argument");
+  mg->level_apply(level, src, dst, (cudaStream_t)stream);
+  EXG_API_END
+}
+
+exg_status exg_mg_smooth(exg_mg* mg, int level, const void* rhs, void* x, int zero_start, void* stream) {
+  EXG_API_BEGIN
+  EXG_CHECK(mg && rhs && x && rhs != x, EXG_ERR_INVALID, "null or aliased argument");
+  mg->level_smooth(level, rhs, x, zero_start != 0, (cudaStream_t)stream);
+  EXG_API_END
+}
+
+exg_status exg_mg_restrict_add(exg_mg* mg, int level, const void* fine, void* coarse, void* stream) {
+  EXG_API_BEGIN
+  EXG_CHECK(mg && fine && coarse, EXG_ERR_INVALID, "null argument");
+  mg->level_restrict_add(level, fine, coarse, (cudaStream_t)stream);
+  EXG_API_END
+}
+
+exg_status exg_mg_prolongate_add(exg_mg* mg, int level, const void* coarse, void* fine, void* stream) {
+  EXG_API_BEGIN
+  EXG_CHECK(mg && fine && coarse, EXG_ERR_INVALID, "null argument");
+  mg->level_prolongate_add(level, coarse, fine, (cudaStream_t)stream);
+  EXG_API_END
+}
+
+exg_status exg_mg_coarse_solve(exg_mg* mg, const void* src, void* dst, void* stream) {
+  EXG_API_BEGIN
+  EXG_CHECK(mg && src && dst && src != dst, EXG_ERR_INVALID, "null or aliased argument");
+  mg->coarse_solve_into(src, dst, (cudaStream_t)stream);
+  EXG_API_END
+}
+
 exg_status exg_mg_info_get(const exg_mg* mg, exg_mg_info* info) {
   EXG_API_BEGIN
   EXG_CHECK(mg && info, EXG_ERR_INVALID, "null argument");

@@ -661,14 +661,9 @@ void exg_mg::smooth(int l, bool zero_start, cudaStream_t s) {
   }
 }
 
-void exg_mg::v_cycle(int l, cudaStream_t s) {
-  MGLevel& L = lv[l];
-  auto mark = [&](int k) {
-    if (tev) EXG_CUDA(cudaEventRecord((*tev)[4 * l + k], s));
-  };
-  mark(0);
-  if (l == 0) {
-    if (prec == EXG_PREC_F32 && coarse_prec == EXG_PREC_F32)
+void exg_mg::coarse_solve(cudaStream_t s) {
+  MGLevel& L = lv[0];
+  if (prec == EXG_PREC_F32 && coarse_prec == EXG_PREC_F32)
       coarse_cg<float, float>((const float*)coarseA, (const float*)coarse_invd, (const float*)L.def, (float*)L.sol,
                               (float*)coarse_x, n_coarse, desc.coarse_rel_tol, desc.coarse_abs_tol,
                               desc.coarse_max_iter, desc.singular, its_dev, s);
@@ -680,6 +675,16 @@ void exg_mg::v_cycle(int l, cudaStream_t s) {
       coarse_cg<double, double>((const double*)coarseA, (const double*)coarse_invd, (const double*)L.def,
                                 (double*)L.sol, (double*)coarse_x, n_coarse, desc.coarse_rel_tol,
                                 desc.coarse_abs_tol, desc.coarse_max_iter, desc.singular, its_dev, s);
+}
+
+void exg_mg::v_cycle(int l, cudaStream_t s) {
+  MGLevel& L = lv[l];
+  auto mark = [&](int k) {
+    if (tev) EXG_CUDA(cudaEventRecord((*tev)[4 * l + k], s));
+  };
+  mark(0);
+  if (l == 0) {
+    coarse_solve(s);
     mark(1);
     return;
   }
@@ -782,6 +787,57 @@ void exg_mg::timed_vmult(const double* src, double* dst, std::vector<float>& ms,
   }
   for (auto& e : ev) cudaEventDestroy(e);
   ++vcycles;
+}
+
+void exg_mg::level_apply(int l, const void* src, void* dst, cudaStream_t s) {
+  EXG_CHECK(l >= 0 && l < (int)lv.size(), EXG_ERR_INVALID, "level out of range");
+  lv[l].op->apply(src, dst, 1, s);
+}
+
+// SmootherBase::vmult (zero_start) / step on level l >= 1: the level's own work vectors are used
+// and their roles restored afterwards, so a captured V-cycle graph stays valid
+void exg_mg::level_smooth(int l, const void* rhs, void* x, bool zero_start, cudaStream_t s) {
+  EXG_CHECK(l >= 1 && l < (int)lv.size(), EXG_ERR_INVALID, "smoothing levels are 1..n_levels-1");
+  MGLevel& L = lv[l];
+  const size_t bytes = (size_t)L.n * psize(prec);
+  void* sol0 = L.sol;
+  void* old0 = L.old;
+  EXG_CUDA(cudaMemcpyAsync(L.def, rhs, bytes, cudaMemcpyDeviceToDevice, s));
+  if (!zero_start) EXG_CUDA(cudaMemcpyAsync(L.sol, x, bytes, cudaMemcpyDeviceToDevice, s));
+  smooth(l, zero_start, s);
+  EXG_CUDA(cudaMemcpyAsync(x, L.sol, bytes, cudaMemcpyDeviceToDevice, s));
+  L.sol = sol0;
+  L.old = old0;
+}
+
+void exg_mg::level_restrict_add(int l, const void* fine, void* coarse, cudaStream_t s) {
+  EXG_CHECK(l >= 1 && l < (int)lv.size(), EXG_ERR_INVALID, "transfers are between levels l-1 and l >= 1");
+  MGLevel& L = lv[l];
+  if (L.ltr)
+    L.ltr->restrict_add(fine, coarse, s);
+  else if (prec == EXG_PREC_F32)
+    restrict_add<float>(L.tr, (const float*)fine, (float*)coarse, s);
+  else
+    restrict_add<double>(L.tr, (const double*)fine, (double*)coarse, s);
+}
+
+void exg_mg::level_prolongate_add(int l, const void* coarse, void* fine, cudaStream_t s) {
+  EXG_CHECK(l >= 1 && l < (int)lv.size(), EXG_ERR_INVALID, "transfers are between levels l-1 and l >= 1");
+  MGLevel& L = lv[l];
+  if (L.ltr)
+    L.ltr->prolongate_add(coarse, fine, s);
+  else if (prec == EXG_PREC_F32)
+    prolongate_add<float>(L.tr, (const float*)coarse, (float*)fine, s);
+  else
+    prolongate_add<double>(L.tr, (const double*)coarse, (double*)fine, s);
+}
+
+void exg_mg::coarse_solve_into(const void* src, void* dst, cudaStream_t s) {
+  MGLevel& L = lv[0];
+  const size_t bytes = (size_t)L.n * psize(prec);
+  EXG_CUDA(cudaMemcpyAsync(L.def, src, bytes, cudaMemcpyDeviceToDevice, s));
+  coarse_solve(s);
+  EXG_CUDA(cudaMemcpyAsync(dst, L.sol, bytes, cudaMemcpyDeviceToDevice, s));
 }
 
 void exg_mg::info(exg_mg_info& out) const {

@@ -140,7 +140,16 @@ struct exg_mg {
   void timed_vmult(const double* src, double* dst, std::vector<float>& ms, cudaStream_t s);
   void info(exg_mg_info& out) const;
 
+  // the level objects behind the reference's component interfaces (level vectors in the
+  // multigrid precision; level 0 = coarsest)
+  void level_apply(int l, const void* src, void* dst, cudaStream_t s);
+  void level_smooth(int l, const void* rhs, void* x, bool zero_start, cudaStream_t s);
+  void level_restrict_add(int l, const void* fine, void* coarse, cudaStream_t s);
+  void level_prolongate_add(int l, const void* coarse, void* fine, cudaStream_t s);
+  void coarse_solve_into(const void* src, void* dst, cudaStream_t s);
+
  private:
+  void coarse_solve(cudaStream_t s);  // lv[0].sol = coarse CG(lv[0].def)
   void v_cycle(int l, cudaStream_t s);
   std::vector<cudaEvent_t>* tev = nullptr;  // 4 events per level while timed_vmult runs
   void smooth(int l, bool zero_start, cudaStream_t s);

@@ -171,6 +171,26 @@ exg_status exg_mg_create(const exg_op* fine, const exg_mg_desc* desc, exg_mg** m
 exg_status exg_mg_destroy(exg_mg* mg);
 exg_status exg_mg_vmult(exg_mg* mg, const double* src, double* dst, void* stream);
 exg_status exg_mg_info_get(const exg_mg* mg, exg_mg_info* info);
+
+/* The multigrid's level objects behind the reference's component interfaces.  Level vectors are
+ * device arrays in the multigrid precision (float when mg_precision = EXG_PREC_F32, else double);
+ * level 0 is the coarsest.  Calls are stream-ordered.
+ *   exg_mg_level_n_dofs: size of level l and whether it is a DG level.
+ *   exg_mg_level_apply: dst = A_l src (the level operator's vmult, operator_base.cpp:156-168).
+ *   exg_mg_smooth: SmootherBase::vmult (zero_start = 1: x = S(rhs) from zero) or ::step
+ *     (zero_start = 0: x updated in place) of the Chebyshev smoother of level l >= 1
+ *     (multigrid/smoothers/smoother_base.h:28-43, chebyshev_smoother.h:79-210).
+ *   exg_mg_restrict_add / exg_mg_prolongate_add: MultigridTransferBase::restrict_and_add
+ *     (coarse += R fine) / prolongate_and_add (fine += P coarse) between levels l-1 and l >= 1
+ *     (multigrid/transfer_base.h:27-41, transfer.cpp:76-96).
+ *   exg_mg_coarse_solve: CoarseGridSolverBase::operator() (coarse_grid_solvers.h:49-59, 157-224):
+ *     dst = coarse CG(src), started from the previous coarse solution as in the V-cycle. */
+exg_status exg_mg_level_n_dofs(const exg_mg* mg, int level, long long* n_dofs, int* is_dg);
+exg_status exg_mg_level_apply(exg_mg* mg, int level, const void* src, void* dst, void* stream);
+exg_status exg_mg_smooth(exg_mg* mg, int level, const void* rhs, void* x, int zero_start, void* stream);
+exg_status exg_mg_restrict_add(exg_mg* mg, int level, const void* fine, void* coarse, void* stream);
+exg_status exg_mg_prolongate_add(exg_mg* mg, int level, const void* coarse, void* fine, void* stream);
+exg_status exg_mg_coarse_solve(exg_mg* mg, const void* src, void* dst, void* stream);
 /* One V-cycle dst = M src run eagerly with CUDA events around each level's work (smoothing,
  * residual and transfers on the way down and up; level 0 = the coarse solve); ms[l] receives the
  * time of level l, coarse first, for up to `capacity` levels; *n_levels the number of levels.

@@ -212,3 +212,68 @@ def test_level_timings_match_vcycle():
     b = torch.empty_like(r)
     mg3.level_timings(r, b)
     assert float(torch.linalg.norm(a - b) / torch.linalg.norm(a)) <= 1e-13
+
+
+def _composed_vcycle(mg, src):
+    """MultigridAlgorithm::v_cycle (multigrid_algorithm.h:172-240) written against the level
+    objects of the C ABI: smoother vmult/step, level vmult, restrict_and_add, coarse solver,
+    prolongate_and_add."""
+    import torch
+
+    nl = mg.info()["n_levels"]
+    dt = mg.level_dtype
+    defs = [torch.zeros(mg.level_n_dofs(l), dtype=dt, device="cuda") for l in range(nl)]
+    sols = [torch.zeros_like(d) for d in defs]
+    defs[-1].copy_(src.to(dt))
+
+    def cycle(l):
+        if l == 0:
+            mg.coarse_solve(sols[0], defs[0])
+            return
+        mg.smooth(l, sols[l], defs[l], zero_start=True)
+        t = torch.empty_like(defs[l])
+        mg.level_vmult(l, t, sols[l])
+        mg.restrict_and_add(l, defs[l - 1], defs[l] - t)
+        cycle(l - 1)
+        mg.prolongate_and_add(l, sols[l], sols[l - 1])
+        mg.smooth(l, sols[l], defs[l], zero_start=False)
+
+    cycle(nl - 1)
+    return sols[-1].double()
+
+
+@pytest.mark.parametrize("mg_type", [E.MG_PH, E.MG_CPH])
+@pytest.mark.parametrize("mg_prec", [E.PREC_F64, E.PREC_F32])
+@pytest.mark.parametrize("curved", [False, True])
+def test_vcycle_from_level_objects(mg_type, mg_prec, curved):
+    """The V-cycle assembled from the exported smoother, transfer, level-operator and coarse-solver
+    entry points reproduces exg_mg_vmult (two fresh preconditioners, so both coarse solvers start
+    from zero; the second input checks the warm start)."""
+    torch = require_gpu()
+    _, m = sine(3, curved, n=4)
+    op = E.LaplaceOperator(m, 3)
+    kw = dict(mg_precision=mg_prec, mg_type=mg_type, use_graph=False)
+    a = E.MultigridPreconditioner(op, **kw)
+    b = E.MultigridPreconditioner(op, **kw)
+    tol = 1e-13 if mg_prec == E.PREC_F64 else 1e-6
+    for seed in (1, 2):
+        r = to_dev(torch, splitmix_uniform(op.n_dofs, seed))
+        ref = a.vmult(op.initialize_dof_vector(), r)
+        got = _composed_vcycle(b, r)
+        assert float(torch.linalg.norm(got - ref) / torch.linalg.norm(ref)) <= tol
+
+
+def test_level_transfers_are_transposes():
+    torch = require_gpu()
+    _, m = sine(3, False, n=4)
+    op = E.LaplaceOperator(m, 3)
+    for mg_type in (E.MG_PH, E.MG_CPH):
+        mg = E.MultigridPreconditioner(op, mg_precision=E.PREC_F64, mg_type=mg_type)
+        for l in range(1, mg.info()["n_levels"]):
+            nf, nc = mg.level_n_dofs(l), mg.level_n_dofs(l - 1)
+            f = to_dev(torch, splitmix_uniform(nf, 3 + l))
+            c = to_dev(torch, splitmix_uniform(nc, 7 + l))
+            Rf = mg.restrict_and_add(l, torch.zeros(nc, dtype=torch.float64, device="cuda"), f)
+            Pc = mg.prolongate_and_add(l, torch.zeros(nf, dtype=torch.float64, device="cuda"), c)
+            lhs, rhs = float(Rf @ c), float(f @ Pc)
+            assert abs(lhs - rhs) <= 1e-11 * max(1.0, abs(lhs))

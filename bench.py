@@ -350,12 +350,19 @@ def run_gpu(args):
 
             x64s, r64 = D.solve_unit_cube_sine(N_CELLS, DEGREE, E.PREC_F64, E.PREC_F64)
             xm, rm = D.solve_unit_cube_sine(N_CELLS, DEGREE, E.PREC_F64E, E.PREC_F32)
+            mixed_diff = float(torch.linalg.norm(xm - x64s) / torch.linalg.norm(x64s))
+            del xm
+            # cphMG (continuous levels below the finest DG level), mixed precision
+            xc, rc = D.solve_unit_cube_sine(N_CELLS, DEGREE, E.PREC_F64E, E.PREC_F32, mg_type=E.MG_CPH)
             line["solve_to_1e-10"] = {
                 "plain_fp64": {"iterations": r64["iterations"], "seconds": r64["wall_seconds"]},
                 "mixed_fp32_graph_vcycle": {"iterations": rm["iterations"], "seconds": rm["wall_seconds"]},
+                "mixed_cphmg": {"iterations": rc["iterations"], "seconds": rc["wall_seconds"],
+                                "solution_rel_diff": float(torch.linalg.norm(xc - x64s) / torch.linalg.norm(x64s))},
                 "speedup": r64["wall_seconds"] / rm["wall_seconds"],
-                "solution_rel_diff": float(torch.linalg.norm(xm - x64s) / torch.linalg.norm(x64s))}
-            del x64s, xm
+                "speedup_cphmg": r64["wall_seconds"] / rc["wall_seconds"],
+                "solution_rel_diff": mixed_diff}
+            del x64s, xc
         line["cpu_baseline"] = cpu_apply_sample(seconds=10.0) if not args.no_cpu_baseline else None
         out = line
         print(json.dumps(out))

@@ -511,14 +511,20 @@ static TransferParams make_transfer(const MGLevel& c, const MGLevel& f) {
 }
 
 exg_mg::exg_mg(const exg_op& fine, const exg_mg_desc& d) : desc(d) {
-  EXG_CHECK(!fine.continuous, EXG_ERR_UNSUPPORTED, "the multigrid's fine operator is the DG operator");
   EXG_CHECK(d.mg_precision == EXG_PREC_F32 || d.mg_precision == EXG_PREC_F64, EXG_ERR_INVALID,
             "mg_precision must be EXG_PREC_F32 or EXG_PREC_F64");
   EXG_CHECK(d.cheb_degree >= 1 && d.eig_iters >= 1, EXG_ERR_INVALID, "bad smoother parameters");
   prec = d.mg_precision;
   coarse_prec = d.coarse_double ? EXG_PREC_F64 : prec;
   EXG_CHECK(d.mg_type == EXG_MG_PH || d.mg_type == EXG_MG_CPH, EXG_ERR_INVALID, "mg_type must be EXG_MG_PH or EXG_MG_CPH");
-  auto list = mg_level_list(fine.mesh.N, fine.degree, std::max(1, d.min_coarse_cells), d.mg_type == EXG_MG_CPH);
+  // a continuous fine operator (the continuous discretization): the cphMG list without its DG top
+  auto list = mg_level_list(fine.mesh.N, fine.degree, std::max(1, d.min_coarse_cells),
+                            d.mg_type == EXG_MG_CPH || fine.continuous);
+  if (fine.continuous) {
+    list.pop_back();
+    EXG_CHECK(fine.lat->mask.pin_first == (d.singular ? 1 : 0), EXG_ERR_INVALID,
+              "the multigrid's singular flag must match the continuous operator's");
+  }
   EXG_CHECK(list.size() <= 32, EXG_ERR_UNSUPPORTED, "too many levels");
   cudaStream_t s = nullptr;
   lv.resize(list.size());

@@ -167,6 +167,9 @@ typedef struct {
  * (MultigridPreconditionerBase::initialize/vmult, multigrid/multigrid_preconditioner_base.cpp:55-95,
  *  673-683; MultigridAlgorithm::v_cycle, multigrid/multigrid_algorithm.h:172-240). */
 exg_status exg_mg_default_desc(exg_mg_desc* desc);
+/* fine: the DG operator (exg_sipg_create), or a continuous operator (exg_continuous_create: the
+ * continuous discretization; levels FE_Q(k) -> ... -> FE_Q(1), then h-coarsening in FE_Q(1),
+ * mg_type ignored, desc->singular must match the operator's). */
 exg_status exg_mg_create(const exg_op* fine, const exg_mg_desc* desc, exg_mg** mg);
 exg_status exg_mg_destroy(exg_mg* mg);
 exg_status exg_mg_vmult(exg_mg* mg, const double* src, double* dst, void* stream);

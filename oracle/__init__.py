@@ -140,6 +140,10 @@ def lib():
         L.orc_cg_dg_map.argtypes = [P, ctypes.POINTER(ctypes.c_long)]
         L.orc_lattice_transfer.argtypes = [ctypes.POINTER(MeshDesc), I, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                            ctypes.c_int, ctypes.c_int, D, D]
+        L.orc_cg_mg_create.restype = P
+        L.orc_cg_mg_create.argtypes = [P, ctypes.POINTER(SolverDesc)]
+        L.orc_cg_solve.restype = ctypes.c_int
+        L.orc_cg_solve.argtypes = [P, P, ctypes.POINTER(SolverDesc), D, D, ctypes.POINTER(SolverResult)]
         L.orc_mg_level_dg.restype = ctypes.c_int
         L.orc_mg_level_dg.argtypes = [P, ctypes.c_int]
         _lib = L
@@ -357,6 +361,23 @@ class ContinuousProblem:
         out = np.empty(self.n_dofs, dtype=np.uint8)
         lib().orc_cg_constrained(self.h, out.ctypes.data_as(ctypes.POINTER(ctypes.c_ubyte)))
         return out.astype(bool)
+
+    def multigrid(self, **kw):
+        """multigrid for the continuous discretization (continuous p- then h-levels)"""
+        mg = Multigrid.__new__(Multigrid)
+        mg.problem = self
+        mg.desc = solver_desc(**kw)
+        mg.h = lib().orc_cg_mg_create(self.h, ctypes.byref(mg.desc))
+        return mg
+
+    def solve(self, b, mg=None, x0=None, **kw):
+        """CG on the continuous operator (preconditioned by `mg` from multigrid(), or none)"""
+        d = solver_desc(**kw)
+        b = np.ascontiguousarray(b, dtype=np.float64)
+        x = np.zeros(self.n_dofs) if x0 is None else np.array(x0, dtype=np.float64)
+        r = SolverResult()
+        lib().orc_cg_solve(self.h, mg.h if mg is not None else None, ctypes.byref(d), _dp(b), _dp(x), ctypes.byref(r))
+        return x, r
 
     def dg_map(self):
         """lattice node of every DG DoF of the same mesh and degree"""

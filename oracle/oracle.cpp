@@ -1785,9 +1785,12 @@ struct Multigrid {
     return std::unique_ptr<LevelOp<T>>(op);
   }
 
-  void setup(const orc_mesh_desc& fine, int degree, double ip, const orc_solver_desc& d) {
+  // continuous_fine: the fine operator is the continuous one (a continuous discretization): the
+  // cphMG level list without its DG top level
+  void setup(const orc_mesh_desc& fine, int degree, double ip, const orc_solver_desc& d, bool continuous_fine = false) {
     desc = d;
-    info = mg_levels(fine, degree, std::max(1, d.min_coarse_cells), d.mg_type == 1);
+    info = mg_levels(fine, degree, std::max(1, d.min_coarse_cells), d.mg_type == 1 || continuous_fine);
+    if (continuous_fine) info.pop_back();
     int L = (int)info.size();
     ops.resize(L);
     smoothers.resize(L);
@@ -2216,12 +2219,56 @@ void orc_transfer(int kc, int kf, const int* Nc, const int* Nf, int restrict_mod
 struct CGHandle {
   ContinuousLaplace<double> d;
   ContinuousLaplace<float> f;
+  orc_mesh_desc mesh;
+  int degree;
 };
 void* orc_cg_create(const orc_mesh_desc* m, int degree, int singular) {
   auto* h = new CGHandle();
   h->d.init(*m, degree, singular != 0);
   h->f.init(*m, degree, singular != 0);
+  h->mesh = *m;
+  h->degree = degree;
   return h;
+}
+// multigrid for the continuous discretization (levels: continuous p- then h-coarsening)
+void* orc_cg_mg_create(void* h, const orc_solver_desc* d) {
+  CGHandle* c = (CGHandle*)h;
+  auto* mg = new MGHandle();
+  mg->is_float = d->mg_float;
+  if (d->mg_float) {
+    mg->mf.reset(new Multigrid<float>());
+    mg->mf->setup(c->mesh, c->degree, 1.0, *d, true);
+  } else {
+    mg->md.reset(new Multigrid<double>());
+    mg->md->setup(c->mesh, c->degree, 1.0, *d, true);
+  }
+  return mg;
+}
+// CG on the continuous operator, preconditioned by such a multigrid (mg may be null: no
+// preconditioner)
+int orc_cg_solve(void* h, void* mg, const orc_solver_desc* d, const double* b, double* x, orc_solver_result* res) {
+  CGHandle* c = (CGHandle*)h;
+  long N = c->d.n_dofs();
+  std::vector<double> bv(b, b + N), xv(x, x + N);
+  auto Aop = [&](const std::vector<double>& in, std::vector<double>& out) { c->d.apply(in.data(), out.data()); };
+  CGResult r;
+  if (mg) {
+    auto Pop = [&](const std::vector<double>& in, std::vector<double>& out) { ((MGHandle*)mg)->vmult(in.data(), out.data()); };
+    r = pcg(Aop, Pop, bv, xv, d->rel_tol, d->abs_tol, d->max_iter, false);
+  } else {
+    auto Pop = [&](const std::vector<double>& in, std::vector<double>& out) { out = in; };
+    r = pcg(Aop, Pop, bv, xv, d->rel_tol, d->abs_tol, d->max_iter, false);
+  }
+  std::copy(xv.begin(), xv.end(), x);
+  if (res) {
+    res->iterations = r.its;
+    res->converged = r.converged;
+    res->r0 = r.r0;
+    res->rn = r.rn;
+    res->rho = r.its > 0 ? std::pow(r.rn / r.r0, 1.0 / r.its) : 0;
+    res->n10 = r.its > 0 ? -10.0 * std::log(10.0) / std::log(res->rho) : 0;
+  }
+  return r.converged ? 0 : 1;
 }
 void orc_cg_destroy(void* h) { delete (CGHandle*)h; }
 long orc_cg_n_dofs(void* h) { return ((CGHandle*)h)->d.n_dofs(); }

@@ -99,8 +99,8 @@ def test_continuous_operator_rejects_dg_only_calls():
     op = E.ContinuousLaplaceOperator(m, 2)
     with pytest.raises(E.ExgError):
         op.quadrature_points()
-    with pytest.raises(E.ExgError):
-        E.MultigridPreconditioner(op)
+    with pytest.raises(E.ExgError):  # singular flag differs from the operator's
+        E.MultigridPreconditioner(op, singular=True)
     with pytest.raises(E.ExgError):
         E.MultigridPreconditioner(op, mg_type=7)
 
@@ -246,4 +246,36 @@ def test_curved_cphmg_sine_solve_golden_and_iterations(k, mg_prec):
     err = p.error(x.cpu().numpy(), O.FN_SINE, 3 * np.pi)
     gold = GOLD["curvilinear"]["relative_l2_error"][k - 1]
     assert abs(err - gold) <= 5e-6 * gold
+
+
+# ---- the continuous discretization: CG on the continuous operator with continuous multigrid
+
+
+@pytest.mark.parametrize("curved", [False, True])
+@pytest.mark.parametrize("k", [2, 4])
+@pytest.mark.parametrize("mg_prec", [E.PREC_F64, E.PREC_F32])
+def test_continuous_discretization_multigrid_solve(curved, k, mg_prec):
+    """The sine problem on FE_Q(k): b = P_c^T of the DG right-hand side (homogeneous data on the
+    constrained nodes); CG + multigrid on FE_Q levels against the oracle (iterations +-1)."""
+    torch = require_gpu()
+    if curved:
+        kw = dict(n_cells=(8, 8, 8), lo=(-1, -1, -1), hi=(1, 1, 1), bc=(0, 1, 0, 0, 0, 0), deform_amp=0.15,
+                  deform_freq=2, deform_left=-1.0, deform_right=1.0, mapping_degree=3)
+        omega = 3 * np.pi
+    else:
+        kw = dict(n_cells=(8, 8, 8))
+        omega = np.pi
+    oc = O.ContinuousProblem(O.mesh_desc(**kw), k)
+    dg = O.Problem(O.mesh_desc(**kw), k)
+    b = np.bincount(oc.dg_map(), weights=dg.rhs(O.FN_SINE, omega), minlength=oc.n_dofs) * ~oc.constrained()
+    op = E.ContinuousLaplaceOperator(E.Mesh(**kw), k)
+    mg = E.MultigridPreconditioner(op, mg_precision=mg_prec)
+    info = mg.info()
+    assert not any(l["dg"] for l in info["levels"]) and info["levels"][-1]["degree"] == k
+    x = op.initialize_dof_vector()
+    its = E.KrylovSolver(op, mg).solve(x, to_dev(torch, b))
+    omg = oc.multigrid(mg_float=1 if mg_prec == E.PREC_F32 else 0)
+    xo, ro = oc.solve(b, mg=omg, rel_tol=1e-10)
+    assert abs(its - ro.iterations) <= 1, (its, ro.iterations)
+    assert rel(x.cpu().numpy(), xo) <= 1e-8
 

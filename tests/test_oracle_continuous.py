@@ -164,3 +164,20 @@ def test_cphmg_solve_matches_phmg_solution(kind, k, mg_float):
         x2 -= x2.mean()
     assert np.linalg.norm(x1 - x2) <= 1e-8 * np.linalg.norm(x1)
     assert r2.iterations <= 40
+
+
+@pytest.mark.parametrize("kind", ["mixed", "curved"])
+def test_continuous_discretization_multigrid(kind):
+    """CG on FE_Q(k) preconditioned by the continuous multigrid (cphMG's list without the DG top)
+    converges to the unpreconditioned CG solution."""
+    m = O.mesh_desc(**mesh_kwargs(kind, 4))
+    k = 3
+    cg = O.ContinuousProblem(m, k)
+    b = splitmix_uniform(cg.n_dofs, 17) * ~cg.constrained()
+    mg = cg.multigrid(mg_float=0)
+    lv = mg.levels()
+    assert not any(l["dg"] for l in lv) and lv[-1]["degree"] == k and lv[-2]["degree"] == 1
+    x, r = cg.solve(b, mg=mg, rel_tol=1e-12)
+    x0, r0 = cg.solve(b, rel_tol=1e-12, max_iter=5000)
+    assert r.converged and r0.converged and r.iterations < r0.iterations
+    assert np.linalg.norm(x - x0) <= 1e-9 * np.linalg.norm(x0)

@@ -118,6 +118,7 @@ EXPORTED_SYMBOLS = [
     "exg_sipg_n_dofs",
     "exg_sipg_info", "exg_sipg_tune", "exg_sipg_set_launch_config", "exg_sipg_apply_f64", "exg_sipg_apply_f32",
     "exg_sipg_residual_f64", "exg_sipg_apply_host_f64", "exg_sipg_inverse_diagonal_f64",
+    "exg_sipg_apply_inverse_block_diagonal_f64", "exg_sipg_apply_inverse_block_diagonal_f32",
     "exg_sipg_inverse_diagonal_f32", "exg_sipg_quadrature_points", "exg_sipg_rhs", "exg_mg_default_desc",
     "exg_mg_create", "exg_mg_destroy", "exg_mg_vmult", "exg_mg_info_get", "exg_mg_level_timings",
     "exg_mg_level_n_dofs", "exg_mg_level_apply", "exg_mg_smooth", "exg_mg_restrict_add", "exg_mg_prolongate_add",
@@ -157,6 +158,8 @@ def load_library(path=LIB_PATH):
         "exg_sipg_apply_f64": [P, P, P, I, P],
         "exg_sipg_apply_f32": [P, P, P, I, P],
         "exg_sipg_residual_f64": [P, P, P, P, P],
+        "exg_sipg_apply_inverse_block_diagonal_f64": [P, P, P, P],
+        "exg_sipg_apply_inverse_block_diagonal_f32": [P, P, P, P],
         "exg_sipg_apply_host_f64": [P, P, P, I, P],
         "exg_sipg_inverse_diagonal_f64": [P, P, P],
         "exg_sipg_inverse_diagonal_f32": [P, P, P],
@@ -358,6 +361,15 @@ class LaplaceOperator:
         _check(_lib.exg_sipg_residual_f64(self.h, _ptr(b), _ptr(x), _ptr(r), _stream(stream)))
         return r
 
+    def apply_inverse_block_diagonal(self, dst, src, stream=None):
+        """dst = blockdiag(A)^-1 src (block Jacobi; Cartesian meshes), in the operator's storage
+        precision (FP32 operators: float vectors, else double)."""
+        f = (_lib.exg_sipg_apply_inverse_block_diagonal_f32 if self.precision == PREC_F32
+             else _lib.exg_sipg_apply_inverse_block_diagonal_f64)
+        _check(f(self.h, _ptr(_sized(src, self.n_dofs, self.dtype, "src")),
+                 _ptr(_sized(dst, self.n_dofs, self.dtype, "dst")), _stream(stream)))
+        return dst
+
     def calculate_inverse_diagonal(self, diag, stream=None):
         f = _lib.exg_sipg_inverse_diagonal_f32 if self.precision == PREC_F32 else _lib.exg_sipg_inverse_diagonal_f64
         _check(f(self.h, _ptr(_sized(diag, self.n_dofs, self.dtype, "diag")), _stream(stream)))
@@ -526,7 +538,7 @@ class MultigridPreconditioner:
 class KrylovSolver:
     """PCG (Krylov::KrylovSolver with SolverCG and ReductionControl)."""
 
-    NONE, JACOBI, MULTIGRID = 0, 1, 2
+    NONE, JACOBI, MULTIGRID, BLOCK_JACOBI = 0, 1, 2, 3
 
     def __init__(self, operator, preconditioner=None, max_iter=10000, abs_tol=1e-20, rel_tol=1e-10, precond=None,
                  device_loop=True):

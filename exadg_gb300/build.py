@@ -32,6 +32,7 @@ SOURCES = [
     "noalloc.cu",
     "cnn.cu",
     "lattice.cu",
+    "block_jacobi.cu",
 ]
 
 

@@ -131,6 +131,21 @@ exg_status exg_sipg_apply_host_f64(exg_op* op, const double* src_host, double* d
   EXG_API_END
 }
 
+static exg_status block_jacobi_apply(exg_op* op, const void* src, void* dst, int prec, void* stream) {
+  EXG_API_BEGIN
+  EXG_CHECK(op && src && dst && src != dst, EXG_ERR_INVALID, "null or aliased argument");
+  op->block_jacobi(prec).apply(src, dst, (cudaStream_t)stream);
+  EXG_API_END
+}
+
+exg_status exg_sipg_apply_inverse_block_diagonal_f64(exg_op* op, const double* src, double* dst, void* stream) {
+  return block_jacobi_apply(op, src, dst, EXG_PREC_F64, stream);
+}
+
+exg_status exg_sipg_apply_inverse_block_diagonal_f32(exg_op* op, const float* src, float* dst, void* stream) {
+  return block_jacobi_apply(op, src, dst, EXG_PREC_F32, stream);
+}
+
 exg_status exg_sipg_residual_f64(exg_op* op, const double* b, const double* x, double* r, void* stream) {
   EXG_API_BEGIN
   EXG_CHECK(op && b && x && r, EXG_ERR_INVALID, "null argument");
@@ -326,6 +341,7 @@ exg_status exg_cg_solve(exg_op* op, exg_mg* mg, const exg_cg_desc* desc, const d
   EXG_CHECK(op && desc && b && x, EXG_ERR_INVALID, "null argument");
   EXG_CHECK(op->precision != EXG_PREC_F32, EXG_ERR_INVALID, "outer CG runs on an FP64 operator");
   EXG_CHECK(desc->precond != 2 || mg, EXG_ERR_INVALID, "multigrid preconditioner requested but mg is NULL");
+  EXG_CHECK(desc->precond >= 0 && desc->precond <= 3, EXG_ERR_INVALID, "unknown preconditioner");
   exg_cg_result r{};
   st = cg_solve(*op, desc->precond == 2 ? mg : nullptr, *desc, b, x, r, (cudaStream_t)stream);
   if (result) *result = r;

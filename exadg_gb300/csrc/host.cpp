@@ -87,6 +87,15 @@ std::unique_ptr<exg_op> exg_op::continuous_level(const MeshInfo& m, int deg, int
   return op;
 }
 
+const BlockJacobi& exg_op::block_jacobi(int prec) {
+  EXG_CHECK(!continuous, EXG_ERR_UNSUPPORTED, "block Jacobi is built for the DG operator");
+  if (!bj || bj->prec != prec) {
+    bj.reset(new BlockJacobi());
+    bj->setup(mesh, fe, ip, prec);
+  }
+  return *bj;
+}
+
 void exg_op::apply(const void* src, void* dst, int n_rhs, cudaStream_t s, const exg::PointEpilogue& ep,
                    long long cell_begin, long long cell_end) const {
   if (continuous) {
@@ -909,6 +918,9 @@ static exg_status cg_solve_device(exg_op& op, exg_mg* mg, const exg_cg_desc& d, 
     if (d.precond == 2) {
       mg->enqueue_vmult(r, z, w.cap);
       dot<double>(r, z, n, red, 4, w.cap);
+    } else if (d.precond == 3) {
+      op.bj->apply(r, z, w.cap);
+      dot<double>(r, z, n, red, 4, w.cap);
     } else {
       precond_dot<double>(dinv, r, z, n, red, 4, w.cap);
     }
@@ -982,6 +994,7 @@ exg_status exg::cg_solve(exg_op& op, exg_mg* mg, const exg_cg_desc& d, const dou
     }
     dinv = w.dinv;
   }
+  if (d.precond == 3) op.block_jacobi(EXG_PREC_F64);  // FP64 work vectors; set up before any capture
   if (d.device_loop) return cg_solve_device(op, mg, d, b, x, res, s);
   EXG_CUDA(cudaStreamSynchronize(s));
   auto t0 = std::chrono::steady_clock::now();
@@ -989,6 +1002,9 @@ exg_status exg::cg_solve(exg_op& op, exg_mg* mg, const exg_cg_desc& d, const dou
   auto P = [&](const double* in, double* out) -> double {
     if (d.precond == 2) {
       mg->vmult(in, out, s);
+      dot<double>(in, out, n, red, 4, s);
+    } else if (d.precond == 3) {
+      op.bj->apply(in, out, s);
       dot<double>(in, out, n, red, 4, s);
     } else {
       precond_dot<double>(d.precond == 1 ? dinv : nullptr, in, out, n, red, 4, s);

@@ -7,6 +7,7 @@
 #include "cg_device.h"
 #include "general.h"
 #include "internal.h"
+#include "block_jacobi.h"
 #include "lattice.h"
 #include "solver_kernels.h"
 
@@ -75,6 +76,9 @@ struct exg_op {
     }
   };
   std::unique_ptr<DgScratch> cdg;
+  // block Jacobi (Cartesian), built on first use in the precision asked for (synchronous)
+  std::unique_ptr<exg::BlockJacobi> bj;
+  const exg::BlockJacobi& block_jacobi(int precision);
   long long n_dofs() const { return continuous ? lat->size() : mesh.n_cells() * n * n * n; }
   // dst = A src on the cells [cell_begin, cell_end) (cell_end < 0: all cells)
   void apply(const void* src, void* dst, int n_rhs, cudaStream_t s,

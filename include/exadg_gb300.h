@@ -97,6 +97,14 @@ exg_status exg_sipg_apply_host_f64(exg_op* op, const double* src_host, double* d
                                    void* stream);
 /* r = b - A x in one kernel (the residual step of the V-cycle and of its residual check,
  * multigrid/multigrid_algorithm.h:155-160, 215-216); r must not alias x.  FP64 storage operators. */
+/* dst = blockdiag(A)^-1 src: the inverse of every cell's diagonal block, cell term plus the cell's
+ * own side of its face terms (OperatorBase::apply_inverse_block_diagonal, operator_base.cpp:820-900;
+ * the BlockJacobi preconditioner, preconditioners/block_jacobi_preconditioner.h).  Cartesian
+ * meshes (at least two cells along a periodic direction); fast diagonalisation of the Kronecker
+ * form, exact up to rounding.  Set up on the first call (synchronous), per precision. */
+exg_status exg_sipg_apply_inverse_block_diagonal_f64(exg_op* op, const double* src, double* dst, void* stream);
+exg_status exg_sipg_apply_inverse_block_diagonal_f32(exg_op* op, const float* src, float* dst, void* stream);
+
 exg_status exg_sipg_residual_f64(exg_op* op, const double* b, const double* x, double* r, void* stream);
 
 /* Autotuner: times the launch variants of the apply kernel (cells per thread block; one thread
@@ -206,7 +214,8 @@ typedef struct {
   int max_iter;        /* 10000 */
   double abs_tol;      /* 1e-20 */
   double rel_tol;      /* 1e-10 */
-  int precond;         /* 0 none, 1 point Jacobi, 2 multigrid (mg handle) */
+  int precond;         /* 0 none, 1 point Jacobi, 2 multigrid (mg handle), 3 block Jacobi
+                        * (Cartesian DG operators; exg_sipg_apply_inverse_block_diagonal_f64) */
   int device_loop;     /* 1: the iterations run as one CUDA-graph launch (a WHILE node over the
                         * captured iteration, scalars and stopping test on the device); 0: host
                         * loop reading the reductions each iteration.  Same arithmetic. */

@@ -106,6 +106,7 @@ def lib():
         L.orc_diagonal_f32.argtypes = [P, F]
         L.orc_diagonal_bruteforce.argtypes = [P, D]
         L.orc_assembled_apply.argtypes = [P, D, D]
+        L.orc_block_jacobi.argtypes = [P, D, D]
         L.orc_rhs.argtypes = [P, ctypes.c_int, ctypes.c_double, ctypes.c_int, D]
         L.orc_error.restype = ctypes.c_double
         L.orc_error.argtypes = [P, D, ctypes.c_int, ctypes.c_double]
@@ -216,6 +217,13 @@ class Problem:
         src = np.ascontiguousarray(src, dtype=np.float64)
         dst = np.empty_like(src)
         lib().orc_assembled_apply(self.h, _dp(src), _dp(dst))
+        return dst
+
+    def block_jacobi(self, src):
+        """dst = blockdiag(A)^-1 src (cell blocks inverted densely)"""
+        src = np.ascontiguousarray(src, dtype=np.float64)
+        dst = np.empty_like(src)
+        lib().orc_block_jacobi(self.h, _dp(src), _dp(dst))
         return dst
 
     def penalty(self):

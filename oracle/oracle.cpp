@@ -2023,6 +2023,62 @@ void orc_penalty(void* h, double* tau) {
 void orc_diagonal_f64(void* h, double* d) { ((Problem*)h)->opd->diagonal(d); }
 void orc_diagonal_f32(void* h, float* d) { ((Problem*)h)->f32().diagonal(d); }
 void orc_diagonal_bruteforce(void* h, double* d) { ((Problem*)h)->opd->diagonal_bruteforce(d); }
+
+// OperatorBase::apply_inverse_block_diagonal (operator_base.cpp:820-900; block Jacobi): per cell the
+// diagonal block A_cc (cell term + the cell's own side of its face terms, neighbours zero) is
+// assembled column by column from unit vectors and inverted by Gauss-Jordan elimination with
+// partial pivoting; dst_c = A_cc^-1 src_c
+void orc_block_jacobi(void* h, const double* src, double* dst) {
+  const Laplace<double>& op = *((Problem*)h)->opd;
+  const long nc = op.n_cells(), n3 = (long)op.n * op.n * op.n, N = op.n_dofs();
+#pragma omp parallel
+  {
+    std::vector<double> full(N, 0.0), buf(op.buf_size()), col(n3), A(n3 * n3), inv(n3 * n3);
+#pragma omp for schedule(static)
+    for (long c = 0; c < nc; ++c) {
+      for (long j = 0; j < n3; ++j) {
+        full[c * n3 + j] = 1.0;
+        std::fill(col.begin(), col.end(), 0.0);
+        op.cell_term(c, full.data() + c * n3, col.data(), buf.data());
+        op.face_terms(c, full.data(), col.data(), buf.data(), HOMOGENEOUS, nullptr);
+        full[c * n3 + j] = 0.0;
+        for (long i = 0; i < n3; ++i) A[i * n3 + j] = col[i];
+      }
+      // Gauss-Jordan on [A | I]
+      for (long i = 0; i < n3; ++i)
+        for (long j = 0; j < n3; ++j) inv[i * n3 + j] = i == j ? 1.0 : 0.0;
+      for (long p = 0; p < n3; ++p) {
+        long piv = p;
+        for (long i = p + 1; i < n3; ++i)
+          if (std::fabs(A[i * n3 + p]) > std::fabs(A[piv * n3 + p])) piv = i;
+        if (piv != p)
+          for (long j = 0; j < n3; ++j) {
+            std::swap(A[p * n3 + j], A[piv * n3 + j]);
+            std::swap(inv[p * n3 + j], inv[piv * n3 + j]);
+          }
+        const double d = A[p * n3 + p];
+        for (long j = 0; j < n3; ++j) {
+          A[p * n3 + j] /= d;
+          inv[p * n3 + j] /= d;
+        }
+        for (long i = 0; i < n3; ++i) {
+          if (i == p) continue;
+          const double f = A[i * n3 + p];
+          if (f == 0.0) continue;
+          for (long j = 0; j < n3; ++j) {
+            A[i * n3 + j] -= f * A[p * n3 + j];
+            inv[i * n3 + j] -= f * inv[p * n3 + j];
+          }
+        }
+      }
+      for (long i = 0; i < n3; ++i) {
+        double acc = 0;
+        for (long j = 0; j < n3; ++j) acc += inv[i * n3 + j] * src[c * n3 + j];
+        dst[c * n3 + i] = acc;
+      }
+    }
+  }
+}
 void orc_assembled_apply(void* h, const double* src, double* dst) { assembled_apply(*((Problem*)h)->opd, src, dst); }
 
 void orc_rhs(void* h, int fn_kind, double omega, int with_f, double* b) {
@@ -2130,6 +2186,8 @@ long orc_mg_coarse_iterations(void* mg) {
 }
 
 // outer CG (Krylov::KrylovSolver::solve -> SolverCG with ReductionControl)
+void orc_block_jacobi(void* h, const double* src, double* dst);
+
 int orc_solve(void* h, const orc_solver_desc* d, const double* b, double* x, orc_solver_result* res) {
   Problem* p = (Problem*)h;
   long N = p->opd->n_dofs();
@@ -2138,6 +2196,9 @@ int orc_solve(void* h, const orc_solver_desc* d, const double* b, double* x, orc
   CGResult r;
   if (d->precond == 0) {
     auto Pop = [&](const std::vector<double>& in, std::vector<double>& out) { out = in; };
+    r = pcg(Aop, Pop, bv, xv, d->rel_tol, d->abs_tol, d->max_iter, false);
+  } else if (d->precond == 3) {  // block Jacobi
+    auto Pop = [&](const std::vector<double>& in, std::vector<double>& out) { orc_block_jacobi(h, in.data(), out.data()); };
     r = pcg(Aop, Pop, bv, xv, d->rel_tol, d->abs_tol, d->max_iter, false);
   } else if (d->precond == 1) {
     std::vector<double> dg(N);

@@ -7,7 +7,7 @@ import pytest
 import exadg_gb300 as E
 import oracle as O
 from tests.gpu_common import pair, rel, require_gpu, to_dev
-from tests.helpers import splitmix_uniform
+from tests.helpers import mesh_kwargs, splitmix_uniform
 
 pytestmark = pytest.mark.gpu
 
@@ -241,3 +241,41 @@ def test_every_dof_written_once_and_deterministic(prec, kind, k):
         op.vmult_host(yh, xh, n_slabs=3)
         torch.cuda.synchronize()
         assert not torch.isnan(yh).any()
+
+
+@pytest.mark.parametrize("kind", ["dirichlet", "mixed", "periodic", "partial_periodic", "anisotropic"])
+@pytest.mark.parametrize("k", [1, 2, 3, 5, 8])
+@pytest.mark.parametrize("prec", [E.PREC_F64, E.PREC_F32])
+def test_block_jacobi_matches_oracle(kind, k, prec):
+    """Fast-diagonalisation block inverse against the oracle's densely inverted cell blocks."""
+    torch = require_gpu()
+    kw = mesh_kwargs(kind, 2 if k >= 5 else 3)
+    p = O.Problem(O.mesh_desc(**kw), k)
+    op = E.LaplaceOperator(E.Mesh(**kw), k, 1.0, prec)
+    r = splitmix_uniform(p.n_dofs, 13)
+    z = op.apply_inverse_block_diagonal(op.initialize_dof_vector(), to_dev(torch, r, op.dtype)).cpu().numpy()
+    assert rel(z, p.block_jacobi(r)) <= (1e-10 if prec == E.PREC_F64 else 1e-4)
+
+
+@pytest.mark.parametrize("device_loop", [True, False])
+def test_cg_block_jacobi_iterations(device_loop):
+    torch = require_gpu()
+    kw = dict(n_cells=(8, 8, 8))
+    p = O.Problem(O.mesh_desc(**kw), 3)
+    op = E.LaplaceOperator(E.Mesh(**kw), 3)
+    b = p.rhs(O.FN_SINE, np.pi)
+    xo, ro = p.solve(b, precond=3)
+    x = op.initialize_dof_vector()
+    its = E.KrylovSolver(op, None, precond=E.KrylovSolver.BLOCK_JACOBI, device_loop=device_loop).solve(
+        x, to_dev(torch, b))
+    assert abs(its - ro.iterations) <= 1, (its, ro.iterations)
+    assert rel(x.cpu().numpy(), xo) <= 1e-8
+
+
+def test_block_jacobi_rejects_curved_and_single_periodic_cell():
+    torch = require_gpu()
+    for kw in (mesh_kwargs("curved", 2), dict(n_cells=(1, 3, 3), periodic=(1, 0, 0))):
+        op = E.LaplaceOperator(E.Mesh(**kw), 2)
+        with pytest.raises(E.ExgError):
+            op.apply_inverse_block_diagonal(op.initialize_dof_vector(), op.initialize_dof_vector())
+    del torch

@@ -74,6 +74,7 @@ class MGDesc(ctypes.Structure):
         ("use_graph", ctypes.c_int),
         ("fuse_smoother", ctypes.c_int),
         ("mg_type", ctypes.c_int),
+        ("smoother_preconditioner", ctypes.c_int),
     ]
 
 
@@ -434,7 +435,8 @@ class MultigridPreconditioner:
 
     def __init__(self, operator, mg_precision=PREC_F32, cheb_degree=5, smoothing_range=20.0, eig_iters=20,
                  coarse_rel_tol=1e-3, coarse_abs_tol=1e-12, coarse_max_iter=10000, coarse_double=False,
-                 min_coarse_cells=2, singular=False, use_graph=True, fuse_smoother=True, mg_type=0):
+                 min_coarse_cells=2, singular=False, use_graph=True, fuse_smoother=True, mg_type=0,
+                 block_jacobi_smoother=False):
         d = MGDesc()
         _check(load_library().exg_mg_default_desc(ctypes.byref(d)))
         d.mg_precision = mg_precision
@@ -450,6 +452,7 @@ class MultigridPreconditioner:
         d.use_graph = int(use_graph)
         d.fuse_smoother = int(fuse_smoother)
         d.mg_type = int(mg_type)
+        d.smoother_preconditioner = 1 if block_jacobi_smoother else 0
         self.desc = d
         self.operator = operator
         h = ctypes.c_void_p()

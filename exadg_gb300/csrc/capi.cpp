@@ -238,6 +238,7 @@ exg_status exg_mg_default_desc(exg_mg_desc* d) {
   d->use_graph = 1;
   d->fuse_smoother = 1;
   d->mg_type = EXG_MG_PH;
+  d->smoother_preconditioner = 0;
   EXG_API_END
 }
 

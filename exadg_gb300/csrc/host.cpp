@@ -478,7 +478,12 @@ static void level_eigen(MGLevel& L, const exg_mg_desc& d, cudaStream_t s) {
   const T* dinv = (const T*)L.invd;
   auto A = [&](const T* in, T* out) { L.op->apply(in, out, 1, s); };
   auto P = [&](const T* in, T* out) -> double {
-    precond_dot<T>(dinv, in, out, n, red, 4, s);
+    if (L.bj) {
+      L.bj->apply(in, out, s);
+      dot<T>(in, out, n, red, 4, s);
+    } else {
+      precond_dot<T>(dinv, in, out, n, red, 4, s);
+    }
     return read_slot(red, 4, s);
   };
   CGStats st = pcg_run<T>(A, P, b, x, n, 0.0, 1e-10, d.eig_iters, true, true, r, z, p, v, red, s);
@@ -565,6 +570,15 @@ exg_mg::exg_mg(const exg_op& fine, const exg_mg_desc& d) : desc(d) {
       L.old = dalloc(bytes);
       L.invd = dalloc(bytes);
       L.op->diagonal(L.invd, true, s);
+      if (d.smoother_preconditioner == 1) {
+        EXG_CHECK(L.dg && L.op->cartesian, EXG_ERR_UNSUPPORTED,
+                  "block-Jacobi smoothing is built for DG levels of Cartesian meshes (phMG)");
+        L.bj = &L.op->block_jacobi(prec);
+        L.ones = dalloc(bytes);
+        L.zeros = dalloc(bytes);
+        vec_fill(L.ones, prec, 1.0, L.n, s);
+        EXG_CUDA(cudaMemsetAsync(L.zeros, 0, bytes, s));
+      }
       if (prec == EXG_PREC_F32)
         level_eigen<float>(L, d, s);
       else
@@ -620,7 +634,7 @@ exg_mg::~exg_mg() {
   if (graph) cudaGraphDestroy(graph);
   if (cap_stream) cudaStreamDestroy(cap_stream);
   for (auto& L : lv)
-    for (void* p : {L.invd, L.sol, L.def, L.t, L.tmp, L.old})
+    for (void* p : {L.invd, L.sol, L.def, L.t, L.tmp, L.old, L.ones, L.zeros})
       if (p) cudaFree(p);
   for (void* p : {coarseA, coarse_invd, coarse_x, (void*)its_dev})
     if (p) cudaFree(p);
@@ -657,6 +671,46 @@ void exg_mg::smooth(int l, bool zero_start, cudaStream_t s) {
     L.op->apply(L.sol, nullptr, 1, s, ep);
     std::swap(L.sol, L.old);
   };
+  if (L.bj) {
+    // Chebyshev on block Jacobi: every step z = P^-1 (def - A sol) and the update with d = 1,
+    // t = 0 in the shared point formula (pr = d (b - t) = z)
+    auto bupd = [&](int mode, double f1, double f2) {
+      if (prec == EXG_PREC_F32)
+        chebyshev_update<float>(mode, (float*)L.sol, (float*)L.old, (const float*)L.t, (const float*)L.zeros,
+                                (const float*)L.ones, f1, f2, L.n, s);
+      else
+        chebyshev_update<double>(mode, (double*)L.sol, (double*)L.old, (const double*)L.t, (const double*)L.zeros,
+                                 (const double*)L.ones, f1, f2, L.n, s);
+    };
+    auto bstep = [&](int mode, double f1, double f2) {
+      L.op->apply(L.sol, L.tmp, 1, s);
+      if (prec == EXG_PREC_F32)
+        rsub<float>((const float*)L.def, (float*)L.tmp, L.n, s);
+      else
+        rsub<double>((const double*)L.def, (double*)L.tmp, L.n, s);
+      L.bj->apply(L.tmp, L.t, s);
+      bupd(mode, f1, f2);
+    };
+    int bfirst;
+    if (zero_start) {
+      L.bj->apply(L.def, L.t, s);
+      bupd(0, 0.0, 1.0 / L.theta);
+      bfirst = 0;
+    } else {
+      bstep(1, 0.0, 1.0 / L.theta);
+      bfirst = 1;
+    }
+    if (deg < 2 || std::fabs(L.delta) < 1e-40) return;
+    double rk = L.delta / L.theta, sg = L.theta / L.delta;
+    for (int k = 0; k < deg - 1; ++k) {
+      double rkp = 1.0 / (2.0 * sg - rk);
+      double f1 = rkp * rk, f2 = 2.0 * rkp / L.delta;
+      rk = rkp;
+      int idx = k + 1 + bfirst;
+      bstep(idx == 1 ? 2 : 3, f1, f2);
+    }
+    return;
+  }
   int first;
   if (zero_start) {
     upd(0, 0.0, 1.0 / L.theta);

@@ -113,6 +113,9 @@ struct MGLevel {
   int eig_its = 0;
   TransferParams tr{};  // transfer from level l-1 to l (l-1 discontinuous)
   std::unique_ptr<LatticeTransfer> ltr;  // transfer from a continuous level l-1
+  const BlockJacobi* bj = nullptr;       // block-Jacobi smoothing: the level's block inverse
+  void* ones = nullptr;                  // block-Jacobi smoothing: unit "diagonal" for the update
+  void* zeros = nullptr;
 };
 }  // namespace exg
 

@@ -155,6 +155,9 @@ typedef struct {
                             * continuous FE_Q(k) level below the finest DG level and coarsening in
                             * the continuous space (multigrid_preconditioner_base.cpp:188-199;
                             * the default of applications/poisson/sine/application.h:167). */
+  int smoother_preconditioner; /* 0: Chebyshev on point Jacobi (PreconditionerSmoother::PointJacobi,
+                                * the default); 1: on block Jacobi (::BlockJacobi; DG levels of
+                                * Cartesian meshes, phMG) */
 } exg_mg_desc;
 
 #define EXG_MG_PH 0

@@ -56,6 +56,7 @@ class SolverDesc(ctypes.Structure):
         ("min_coarse_cells", ctypes.c_int),
         ("singular", ctypes.c_int),
         ("mg_type", ctypes.c_int),
+        ("smoother_block", ctypes.c_int),
     ]
 
 

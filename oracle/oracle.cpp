@@ -171,6 +171,7 @@ typedef struct {
   int min_coarse_cells;  // stop h-coarsening at this many cells per direction (2)
   int singular;          // subtract mean in the coarse solve (pure Neumann / periodic)
   int mg_type;           // 0: phMG (DG on every level), 1: cphMG (continuous levels below the finest)
+  int smoother_block;    // Chebyshev preconditioned by block Jacobi (DG levels) instead of point Jacobi
 } orc_solver_desc;
 
 typedef struct {
@@ -1573,11 +1574,82 @@ static std::vector<LevelInfo> mg_levels(const orc_mesh_desc& fine, int degree, i
   return lv;
 }
 
+// the inverse cell-diagonal blocks of a DG operator (block Jacobi, operator_base.cpp:820-900):
+// each block (cell term + the cell's own side of its face terms) assembled from unit vectors in
+// double, inverted by Gauss-Jordan elimination with partial pivoting, applied in Number
+static void invert_dense(long n, std::vector<double>& A, std::vector<double>& inv) {
+  inv.assign(n * n, 0.0);
+  for (long i = 0; i < n; ++i) inv[i * n + i] = 1.0;
+  for (long p = 0; p < n; ++p) {
+    long piv = p;
+    for (long i = p + 1; i < n; ++i)
+      if (std::fabs(A[i * n + p]) > std::fabs(A[piv * n + p])) piv = i;
+    if (piv != p)
+      for (long j = 0; j < n; ++j) {
+        std::swap(A[p * n + j], A[piv * n + j]);
+        std::swap(inv[p * n + j], inv[piv * n + j]);
+      }
+    const double d = A[p * n + p];
+    for (long j = 0; j < n; ++j) {
+      A[p * n + j] /= d;
+      inv[p * n + j] /= d;
+    }
+    for (long i = 0; i < n; ++i) {
+      if (i == p) continue;
+      const double f = A[i * n + p];
+      if (f == 0.0) continue;
+      for (long j = 0; j < n; ++j) {
+        A[i * n + j] -= f * A[p * n + j];
+        inv[i * n + j] -= f * inv[p * n + j];
+      }
+    }
+  }
+}
+
+template <class Number>
+struct BlockInverse {
+  long nc = 0, n3 = 0;
+  std::vector<Number> inv;  // [cell][n3][n3]
+  void init(const Laplace<double>& op) {
+    nc = op.n_cells();
+    n3 = (long)op.n * op.n * op.n;
+    inv.resize(nc * n3 * n3);
+    const long N = op.n_dofs();
+#pragma omp parallel
+    {
+      std::vector<double> full(N, 0.0), buf(op.buf_size()), col(n3), A(n3 * n3), iv;
+#pragma omp for schedule(static)
+      for (long c = 0; c < nc; ++c) {
+        for (long j = 0; j < n3; ++j) {
+          full[c * n3 + j] = 1.0;
+          std::fill(col.begin(), col.end(), 0.0);
+          op.cell_term(c, full.data() + c * n3, col.data(), buf.data());
+          op.face_terms(c, full.data(), col.data(), buf.data(), HOMOGENEOUS, nullptr);
+          full[c * n3 + j] = 0.0;
+          for (long i = 0; i < n3; ++i) A[i * n3 + j] = col[i];
+        }
+        invert_dense(n3, A, iv);
+        for (long i = 0; i < n3 * n3; ++i) inv[c * n3 * n3 + i] = (Number)iv[i];
+      }
+    }
+  }
+  void apply(const Number* src, Number* dst) const {
+#pragma omp parallel for schedule(static)
+    for (long c = 0; c < nc; ++c)
+      for (long i = 0; i < n3; ++i) {
+        Number acc = 0;
+        for (long j = 0; j < n3; ++j) acc += inv[(c * n3 + i) * n3 + j] * src[c * n3 + j];
+        dst[c * n3 + i] = acc;
+      }
+  }
+};
+
 template <class Number>
 struct Chebyshev {
   // deal.II PreconditionChebyshev (first kind), chebyshev_smoother.h:79-210
   const LevelOp<Number>* A;
   std::vector<Number> inv_diag;
+  const BlockInverse<Number>* block = nullptr;  // PreconditionerSmoother::BlockJacobi when set
   int degree;
   double theta, delta, lambda_max, lambda_min;
   int eig_its;
@@ -1606,7 +1678,10 @@ struct Chebyshev {
     for (long i = 0; i < N; ++i) b[i] -= (Number)mean;
     auto Aop = [&](const std::vector<Number>& in, std::vector<Number>& out) { op->apply(in.data(), out.data()); };
     auto Pop = [&](const std::vector<Number>& in, std::vector<Number>& out) {
-      for (long i = 0; i < N; ++i) out[i] = inv_diag[i] * in[i];
+      if (block)
+        block->apply(in.data(), out.data());
+      else
+        for (long i = 0; i < N; ++i) out[i] = inv_diag[i] * in[i];
     };
     CGResult r = pcg(Aop, Pop, b, x, 0.0, 1e-10, eig_iters, true, true);
     eig_its = r.its;
@@ -1622,15 +1697,28 @@ struct Chebyshev {
   // x_{k+1} = (1+f1) x_k - f1 x_{k-1} + f2 P (b - A x_k)
   void iterate(std::vector<Number>& x, const std::vector<Number>& b, bool zero_start) const {
     long N = (long)x.size();
+    // block Jacobi: t2 = P^-1 (b - t1) for the update (deal.II's preconditioner.vmult of the residual)
+    auto block_residual = [&](bool with_t1) {
+      for (long i = 0; i < N; ++i) t2[i] = with_t1 ? b[i] - t1[i] : b[i];
+      std::vector<Number> z(N);
+      block->apply(t2.data(), z.data());
+      t2.swap(z);
+    };
     int first;
     if (zero_start) {
-      for (long i = 0; i < N; ++i) x[i] = (Number)(1.0 / theta) * inv_diag[i] * b[i];
+      if (block) {
+        block_residual(false);
+        for (long i = 0; i < N; ++i) x[i] = (Number)(1.0 / theta) * t2[i];
+      } else {
+        for (long i = 0; i < N; ++i) x[i] = (Number)(1.0 / theta) * inv_diag[i] * b[i];
+      }
       first = 0;
     } else {
       A->apply(x.data(), t1.data());
       Number f2 = (Number)(1.0 / theta);
+      if (block) block_residual(true);
       for (long i = 0; i < N; ++i) {
-        Number upd = f2 * inv_diag[i] * (b[i] - t1[i]);
+        Number upd = block ? f2 * t2[i] : f2 * inv_diag[i] * (b[i] - t1[i]);
         old[i] = x[i];
         x[i] = x[i] + upd;
       }
@@ -1644,8 +1732,9 @@ struct Chebyshev {
       Number f1 = (Number)(rhokp * rhok), f2 = (Number)(2.0 * rhokp / delta);
       rhok = rhokp;
       int idx = k + 1 + first;
+      if (block) block_residual(true);
       for (long i = 0; i < N; ++i) {
-        Number pr = inv_diag[i] * (b[i] - t1[i]);
+        Number pr = block ? t2[i] : inv_diag[i] * (b[i] - t1[i]);
         Number xn;
         if (idx == 1)
           xn = (Number(1) + f1) * x[i] + f2 * pr;  // x_{-1} = 0 after a zero start
@@ -1762,6 +1851,7 @@ struct Multigrid {
   std::vector<LevelInfo> info;
   std::vector<std::unique_ptr<LevelOp<Number>>> ops;
   std::vector<std::unique_ptr<Chebyshev<Number>>> smoothers;
+  std::vector<std::unique_ptr<BlockInverse<Number>>> blocks;  // block-Jacobi smoothing
   std::vector<std::unique_ptr<TransferBase<Number>>> transfers;  // transfers[l] between l-1 and l
   std::unique_ptr<LevelOp<double>> coarse_op_d;  // coarse operator in double (optional)
   std::vector<double> coarse_inv_diag_d;
@@ -1808,6 +1898,16 @@ struct Multigrid {
       t[l].assign(N, Number(0));
       if (l > 0) {
         smoothers[l].reset(new Chebyshev<Number>());
+        if (d.smoother_block) {  // block Jacobi is defined for DG levels (operator_base.cpp:653)
+          if (!info[l].dg) throw std::runtime_error("block-Jacobi smoothing needs DG levels");
+          blocks.resize(L);
+          auto g = make_geometry(make_mesh(md), info[l].degree + 1);
+          Laplace<double> opd;
+          opd.init(g, info[l].degree, ip);
+          blocks[l].reset(new BlockInverse<Number>());
+          blocks[l]->init(opd);
+          smoothers[l]->block = blocks[l].get();
+        }
         smoothers[l]->setup(ops[l].get(), d.cheb_degree, d.smoothing_range, d.eig_iters);
         const LevelInfo &ci = info[l - 1], &fi = info[l];
         if (ci.dg) {
@@ -2128,6 +2228,7 @@ void orc_default_solver_desc(orc_solver_desc* d) {
   d->min_coarse_cells = 2;
   d->singular = 0;
   d->mg_type = 0;
+  d->smoother_block = 0;
 }
 
 // multigrid handle (templated on the V-cycle precision)

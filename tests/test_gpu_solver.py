@@ -277,3 +277,51 @@ def test_level_transfers_are_transposes():
             Pc = mg.prolongate_and_add(l, torch.zeros(nf, dtype=torch.float64, device="cuda"), c)
             lhs, rhs = float(Rf @ c), float(f @ Pc)
             assert abs(lhs - rhs) <= 1e-11 * max(1.0, abs(lhs))
+
+
+@pytest.mark.parametrize("mg_prec", [E.PREC_F64, E.PREC_F32])
+@pytest.mark.parametrize("graph", [True, False])
+def test_block_jacobi_smoother_vcycle_matches_oracle(mg_prec, graph):
+    """Chebyshev preconditioned by block Jacobi (PreconditionerSmoother::BlockJacobi)."""
+    torch = require_gpu()
+    from tests.helpers import mesh_kwargs
+
+    kw = mesh_kwargs("mixed", 4)
+    p = O.Problem(O.mesh_desc(**kw), 3)
+    op = E.LaplaceOperator(E.Mesh(**kw), 3)
+    mg = E.MultigridPreconditioner(op, mg_precision=mg_prec, block_jacobi_smoother=True, use_graph=graph)
+    omg = O.Multigrid(p, mg_float=1 if mg_prec == E.PREC_F32 else 0, smoother_block=1)
+    for g, o in zip(mg.info()["levels"], omg.levels()):
+        if o["eig_iters"]:
+            assert g["lambda_max"] == pytest.approx(o["lambda_max"], rel=1e-9 if mg_prec == E.PREC_F64 else 1e-4)
+    for seed in (1, 2):
+        r = splitmix_uniform(p.n_dofs, seed)
+        z = mg.vmult(op.initialize_dof_vector(), to_dev(torch, r))
+        # FP32: the GPU applies the block inverse by fast diagonalisation, the oracle by a dense
+        # inverse; both in float, so the smoother's polynomial sees different rounding (1e-4 level)
+        assert rel(z.cpu().numpy(), omg.vmult(r)) <= (1e-9 if mg_prec == E.PREC_F64 else 2e-4)
+
+
+@pytest.mark.parametrize("k", [3, 4])
+def test_block_jacobi_smoother_solve_iterations(k):
+    torch = require_gpu()
+    p, m = sine(k, False)
+    op = E.LaplaceOperator(m, k)
+    mg = E.MultigridPreconditioner(op, mg_precision=E.PREC_F32, block_jacobi_smoother=True)
+    b = p.rhs(O.FN_SINE, 3 * np.pi)
+    x = op.initialize_dof_vector()
+    its = E.KrylovSolver(op, mg).solve(x, to_dev(torch, b))
+    xo, ro = O.Multigrid(p, mg_float=1, smoother_block=1).solve(b)
+    assert abs(its - ro.iterations) <= 1, (its, ro.iterations)
+    gold = GOLD["cartesian"]["relative_l2_error"][k - 1]
+    assert abs(p.error(x.cpu().numpy(), O.FN_SINE, 3 * np.pi) - gold) <= 5e-6 * gold
+
+
+def test_block_jacobi_smoother_rejects_continuous_and_curved_levels():
+    require_gpu()
+    _, m = sine(3, False, n=4)
+    with pytest.raises(E.ExgError):
+        E.MultigridPreconditioner(E.LaplaceOperator(m, 3), mg_type=E.MG_CPH, block_jacobi_smoother=True)
+    _, mc = sine(3, True, n=4)
+    with pytest.raises(E.ExgError):
+        E.MultigridPreconditioner(E.LaplaceOperator(mc, 3), block_jacobi_smoother=True)

@@ -89,11 +89,13 @@ std::unique_ptr<exg_op> exg_op::continuous_level(const MeshInfo& m, int deg, int
 
 const BlockJacobi& exg_op::block_jacobi(int prec) {
   EXG_CHECK(!continuous, EXG_ERR_UNSUPPORTED, "block Jacobi is built for the DG operator");
-  if (!bj || bj->prec != prec) {
-    bj.reset(new BlockJacobi());
-    bj->setup(mesh, fe, ip, prec);
+  const int slot = prec == EXG_PREC_F32 ? 0 : 1;
+  if (!bj[slot]) {
+    std::unique_ptr<BlockJacobi> b(new BlockJacobi());
+    b->setup(mesh, fe, ip, prec == EXG_PREC_F32 ? EXG_PREC_F32 : EXG_PREC_F64);
+    bj[slot] = std::move(b);
   }
-  return *bj;
+  return *bj[slot];
 }
 
 void exg_op::apply(const void* src, void* dst, int n_rhs, cudaStream_t s, const exg::PointEpilogue& ep,
@@ -973,7 +975,7 @@ static exg_status cg_solve_device(exg_op& op, exg_mg* mg, const exg_cg_desc& d, 
       mg->enqueue_vmult(r, z, w.cap);
       dot<double>(r, z, n, red, 4, w.cap);
     } else if (d.precond == 3) {
-      op.bj->apply(r, z, w.cap);
+      op.bj[1]->apply(r, z, w.cap);
       dot<double>(r, z, n, red, 4, w.cap);
     } else {
       precond_dot<double>(dinv, r, z, n, red, 4, w.cap);
@@ -1058,7 +1060,7 @@ exg_status exg::cg_solve(exg_op& op, exg_mg* mg, const exg_cg_desc& d, const dou
       mg->vmult(in, out, s);
       dot<double>(in, out, n, red, 4, s);
     } else if (d.precond == 3) {
-      op.bj->apply(in, out, s);
+      op.bj[1]->apply(in, out, s);
       dot<double>(in, out, n, red, 4, s);
     } else {
       precond_dot<double>(d.precond == 1 ? dinv : nullptr, in, out, n, red, 4, s);

@@ -76,8 +76,9 @@ struct exg_op {
     }
   };
   std::unique_ptr<DgScratch> cdg;
-  // block Jacobi (Cartesian), built on first use in the precision asked for (synchronous)
-  std::unique_ptr<exg::BlockJacobi> bj;
+  // block Jacobi (Cartesian), one instance per precision (FP32, FP64) built on first use
+  // (synchronous) and kept: captured graphs hold their device pointers
+  std::unique_ptr<exg::BlockJacobi> bj[2];
   const exg::BlockJacobi& block_jacobi(int precision);
   long long n_dofs() const { return continuous ? lat->size() : mesh.n_cells() * n * n * n; }
   // dst = A src on the cells [cell_begin, cell_end) (cell_end < 0: all cells)

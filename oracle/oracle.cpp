@@ -25,6 +25,11 @@
 //   * coarse CG + Jacobi                              multigrid/coarse_grid_solvers.h:157-224
 //   * outer CG (deal.II SolverCG + ReductionControl)  solvers/iterative_solvers_dealii_wrapper.h:136-221
 //   * relative L2 error with QGauss(k+3)              postprocessor/error_calculation.cpp:38-110
+//   * cphMG level list, continuous FE_Q levels and     multigrid/multigrid_preconditioner_base.cpp:
+//     their constraints, c/p/h transfers of the        188-199,520-545, multigrid/constraints.h:
+//     continuous levels                                130-197, operators/operator_base.cpp:264-310
+//   * block Jacobi (dense cell-block inverses) and     operators/operator_base.cpp:820-900,
+//     Chebyshev smoothing on it                         multigrid/smoothers/chebyshev_smoother.h
 //
 // deal.II (>= 9.7, not vendored) supplies FEEvaluation, SolverCG, PreconditionChebyshev and
 // MGTwoLevelTransfer; their published algorithms are restated here in plain loops.
@@ -32,7 +37,8 @@
 // Parity pin: the relative L2 errors of the sine application (Cartesian and curvilinear, 8^3
 // cells, k = 1..7, applications/poisson/sine/tests/{cartesian,curvilinear}.output) are reproduced
 // by tests/test_oracle_golden.py.  An independent assembled-matrix apply cross-checks the
-// sum-factorised apply on small meshes.
+// sum-factorised apply on small meshes.  The continuous operator is pinned to the DG operator by
+// the Galerkin identity A_CG = P_c^T A_DG P_c (tests/test_oracle_continuous.py).
 //
 // Ordering: cells lexicographic (x fastest), DoFs lexicographic within a cell (x fastest).
 // ============================================================================================

@@ -3,9 +3,8 @@
 //
 // Who needs it: callers that must not allocate or free device memory while they run --
 // a time loop that keeps kernels of other streams in flight (cudaMalloc / cudaFree synchronise
-// the device), host frameworks whose memory pool owns the whole device, and code that is being
-// captured into a CUDA graph.  They give up generality: the problem size is capped and calls
-// share one scratch array.
+// the device), and host frameworks whose memory pool owns the whole device.  They give up
+// generality: the problem size is capped and calls share one scratch array.
 //
 // Scratch: kNoallocMaxDofs doubles for each of five work vectors (r, z, p, v, inverse diagonal)
 // plus the reduction partials -- about 20 MiB held by every GPU that loads the library until the
@@ -64,6 +63,10 @@ static exg_status cg_solve_noalloc(exg_op& op, const exg_cg_desc& d, const doubl
             "exg_cg_solve_noalloc: problem has more DoFs than the static scratch holds (524288)");
   EXG_CHECK(d.precond == 0 || d.precond == 1, EXG_ERR_UNSUPPORTED,
             "exg_cg_solve_noalloc supports precond 0 (none) and 1 (point Jacobi)");
+  // the diagonal of a continuous operator on a Cartesian mesh is computed through a temporary
+  // device table, which would allocate
+  EXG_CHECK(!(d.precond == 1 && op.continuous && op.cartesian), EXG_ERR_UNSUPPORTED,
+            "exg_cg_solve_noalloc: point Jacobi on a continuous Cartesian operator would allocate");
   unsigned char* base = noalloc_scratch();
   double* r = (double*)(base + 0 * kNoallocVecBytes);
   double* z = (double*)(base + 1 * kNoallocVecBytes);

@@ -294,8 +294,9 @@ exg_status exg_dg_ls_step(const double* r, const double* Ae, const double* e, co
 exg_status exg_dg_pack_diff(const double* a, const double* b, double inv_scale, int dofs_per_cell,
                             long long n_cells, float* t, void* stream);
 
-/* The same point-Jacobi / unpreconditioned CG as exg_cg_solve (desc->precond 0 or 1), but it
- * allocates nothing: its work vectors live in one statically allocated device array of about
+/* The same point-Jacobi / unpreconditioned CG as exg_cg_solve (desc->precond 0 or 1; point Jacobi
+ * is refused for a continuous operator on a Cartesian mesh, whose diagonal set-up would allocate),
+ * but it allocates nothing: its work vectors live in one statically allocated device array of about
  * 20 MiB that every GPU loading this library holds until the process exits.  For callers that
  * cannot call cudaMalloc / cudaFree while they run (a time loop with other streams in flight --
  * both calls synchronise the device --, a framework whose pool owns the device memory).

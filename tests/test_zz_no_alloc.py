@@ -59,3 +59,21 @@ def test_noalloc_rejects_oversized_problem():
                                 ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert st == E.EXG_ERR_INVALID
     assert b"524288" in L.exg_last_error()
+
+
+def test_noalloc_refuses_point_jacobi_on_continuous_cartesian_operator():
+    """That diagonal set-up would need a temporary device allocation, so the call is refused."""
+    torch = require_gpu()
+    L = E.load_library()
+    op = E.ContinuousLaplaceOperator(E.Mesh(4), 2)
+    d = E.CGDesc()
+    L.exg_cg_default_desc(ctypes.byref(d))
+    d.precond = 1
+    b = op.initialize_dof_vector()
+    x = op.initialize_dof_vector()
+    st = L.exg_cg_solve_noalloc(op.h, ctypes.byref(d), ctypes.c_void_p(b.data_ptr()),
+                                ctypes.c_void_p(x.data_ptr()), None,
+                                ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == E.EXG_ERR_UNSUPPORTED
+    assert b"allocate" in L.exg_last_error()
+

@@ -89,3 +89,27 @@ def test_mg_preconditioned_cg_converges_fast():
     lv = mg.levels()
     assert [l["degree"] for l in lv] == [1, 1, 1, 2, 4]
     assert [l["n_cells"][0] for l in lv] == [2, 4, 8, 8, 8]
+
+
+@pytest.mark.parametrize("kind", ["mixed", "periodic", "curved"])
+def test_block_jacobi_inverts_the_cell_blocks(kind):
+    """The oracle's block Jacobi (dense cell-block inverses) undoes the operator's diagonal blocks,
+    which are obtained here independently as cell-restricted applies of the full operator."""
+    p = O.Problem(O.mesh_desc(**mesh_kwargs(kind, 2)), 2)
+    x = splitmix_uniform(p.n_dofs, 3)
+    n3 = 27
+    bx = np.zeros_like(x)
+    for c in range(p.n_dofs // n3):
+        v = np.zeros_like(x)
+        v[c * n3:(c + 1) * n3] = x[c * n3:(c + 1) * n3]
+        bx[c * n3:(c + 1) * n3] = p.apply(v)[c * n3:(c + 1) * n3]
+    assert np.linalg.norm(p.block_jacobi(bx) - x) <= 1e-12 * np.linalg.norm(x)
+
+
+def test_block_jacobi_smoothed_multigrid_converges():
+    p = O.Problem(O.mesh_desc(**mesh_kwargs("mixed", 4)), 3)
+    b = splitmix_uniform(p.n_dofs, 5)
+    x1, r1 = p.solve(b, smoother_block=0, mg_float=0)
+    x2, r2 = p.solve(b, smoother_block=1, mg_float=0)
+    assert r1.converged and r2.converged and r2.iterations <= r1.iterations + 1
+    assert np.linalg.norm(x1 - x2) <= 1e-8 * np.linalg.norm(x1)
